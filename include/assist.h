@@ -1,0 +1,283 @@
+/*
+ * assist.h -- C ABI of libassist_gb300: ASSIST's plugin surface for the
+ * test-particle equations of motion, backed by sm_103a kernels.
+ *
+ * Every declaration below replaces the ASSIST v1.2.0 interface cited beside it
+ * (paths are relative to the ASSIST source tree).  Struct layouts that the
+ * ASSIST ctypes wrapper mirrors (assist/ephem.py:95-120, assist/extras.py:84-101)
+ * keep ASSIST's member order and types so those mirrors read them unchanged.
+ *
+ * Beyond ASSIST's own surface this header adds the batched entry points
+ * (assist_gb300_*) through which independent particles with their own
+ * adaptive IAS15 steps are integrated in one persistent device kernel.
+ */
+#ifndef ASSIST_GB300_ASSIST_H
+#define ASSIST_GB300_ASSIST_H
+
+#include <stdint.h>
+#include <stddef.h>
+#include <stdio.h>
+#include "rebound.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+extern const char* assist_build_str;      /* src/assist.h:36 */
+extern const char* assist_version_str;    /* src/assist.h:37 */
+extern const char* assist_githash_str;    /* src/assist.h:38 */
+
+/* src/assist.h:53-58 */
+typedef enum {
+    FILE_FORMAT_VALID_BSP = 0,
+    FILE_FORMAT_ASCII_BIN = 2,
+    FILE_FORMAT_UNKNOWN = 3
+} ephemeris_file_format_t;
+
+int assist_detect_ascii_bin_signature(int fd);                               /* src/assist.h:65 */
+ephemeris_file_format_t assist_detect_ephemeris_file_format(int fd);          /* src/assist.h:68 */
+int assist_discover_planets_path(char* out_path, size_t out_path_size,
+                                 const char* assist_dir);                     /* src/assist.h:72 */
+
+/* Force selection bits, src/assist.h:76-87 */
+enum ASSIST_FORCES {
+    ASSIST_FORCE_NONE               = 0,
+    ASSIST_FORCE_SUN                = 0x01,
+    ASSIST_FORCE_PLANETS            = 0x02,
+    ASSIST_FORCE_ASTEROIDS          = 0x04,
+    ASSIST_FORCE_NON_GRAVITATIONAL  = 0x08,
+    ASSIST_FORCE_EARTH_HARMONICS    = 0x10,
+    ASSIST_FORCE_SUN_HARMONICS      = 0x20,
+    ASSIST_FORCE_GR_EIH             = 0x40,
+    ASSIST_FORCE_GR_SIMPLE          = 0x80,
+    ASSIST_FORCE_GR_POTENTIAL       = 0x100,
+};
+
+/* Status codes, src/assist.h:90-98; messages in assist_error_messages[]. */
+enum ASSIST_STATUS {
+    ASSIST_SUCCESS,
+    ASSIST_ERROR_EPHEM_FILE,
+    ASSIST_ERROR_AST_FILE,
+    ASSIST_ERROR_NAST,
+    ASSIST_ERROR_NEPHEM,
+    ASSIST_ERROR_COVERAGE,
+    ASSIST_ERROR_N,
+};
+
+extern const char* assist_error_messages[];   /* src/assist.c:52-59 */
+extern const int assist_error_messages_N;     /* src/assist.c:60 */
+
+/* Body indices, src/assist.h:102-116.  Asteroids follow at 11.. */
+enum ASSIST_BODY {
+    ASSIST_BODY_SUN         = 0,
+    ASSIST_BODY_MERCURY     = 1,
+    ASSIST_BODY_VENUS       = 2,
+    ASSIST_BODY_EARTH       = 3,
+    ASSIST_BODY_MOON        = 4,
+    ASSIST_BODY_MARS        = 5,
+    ASSIST_BODY_JUPITER     = 6,
+    ASSIST_BODY_SATURN      = 7,
+    ASSIST_BODY_URANUS      = 8,
+    ASSIST_BODY_NEPTUNE     = 9,
+    ASSIST_BODY_PLUTO       = 10,
+    ASSIST_BODY_NPLANETS    = 11,
+};
+
+struct ascii_s;
+struct spk_s;
+
+/* Ephemeris handle, src/assist.h:125-155 (layout mirrored by assist/ephem.py:95-120).
+ * `planets_calc` keeps its slot for layout; this library evaluates bodies on the
+ * device and leaves it pointing at a host dispatcher that launches the kernel. */
+struct assist_ephem {
+    double jd_ref;
+    struct spk_s* spk_planets;
+    struct spk_s* spk_asteroids;
+    struct ascii_s* ascii_planets;
+    int planets_source;
+    enum ASSIST_STATUS (*planets_calc)(const struct assist_ephem*, double, double, int,
+                                       double* const,
+                                       double* const, double* const, double* const,
+                                       double* const, double* const, double* const,
+                                       double* const, double* const, double* const);
+    int spk_target_index[ASSIST_BODY_NPLANETS];
+    int spk_emb_index;
+    double AU;
+    double EMRAT;
+    double J2E;
+    double J3E;
+    double J4E;
+    double J2SUN;
+    double RE;
+    double CLIGHT;
+    double ASUN;
+    double Re_eq;
+    double Rs_eq;
+    double c_AU_per_day;
+    double c_squared;
+    double over_c_squared;
+};
+
+/* src/assist.h:157-168 */
+struct assist_cache_item {
+    double GM;
+    double x, y, z;
+    double vx, vy, vz;
+    double ax, ay, az;
+};
+
+/* src/assist.h:171-175.  Kept for layout; the device path evaluates every
+ * body once per distinct time and needs no host-side cache. */
+struct assist_ephem_cache {
+    double* t;
+    double dt_sign;
+    struct assist_cache_item* items;
+};
+
+/* Per-simulation extras, src/assist.h:177-195 (mirrored by assist/extras.py:84-101). */
+struct assist_extras {
+    struct reb_simulation* sim;
+    struct assist_ephem* ephem;
+    struct assist_ephem_cache* ephem_cache;
+    int extras_should_free_ephem;
+    int geocentric;
+    struct reb_particle* last_state;
+    struct reb_particle* current_state;
+    double* particle_params;
+    int steps_done;
+    int forces;
+    int gr_eih_sources;
+    double alpha;
+    double nk;
+    double nm;
+    double nn;
+    double r0;
+};
+
+struct assist_extras* assist_attach(struct reb_simulation* sim, struct assist_ephem* ephem);  /* src/assist.h:202 */
+void assist_free(struct assist_extras* assist);                                              /* src/assist.h:209 */
+void assist_ephem_free(struct assist_ephem* ephem);                                          /* src/assist.h:211 */
+void assist_detach(struct reb_simulation* sim, struct assist_extras* assist);                /* src/assist.h:218 */
+void assist_error(struct assist_extras* assist, const char* const msg);                      /* src/assist.h:227 */
+int assist_interpolate_simulation(struct reb_simulation* sim1, struct reb_simulation* sim2, double h);  /* src/assist.h:230 */
+void assist_integrate_or_interpolate(struct assist_extras* ax, double t);                    /* src/assist.h:232 */
+struct reb_particle assist_get_particle(const struct assist_ephem* ephem, const int particle_id, const double t);  /* src/assist.h:235 */
+struct reb_particle assist_get_particle_with_error(const struct assist_ephem* ephem, const int particle_id,
+                                                   const double t, int* error);              /* src/assist.h:245 */
+void assist_ephem_time_bounds(const struct assist_ephem* ephem, double* t_beg, double* t_end);  /* src/assist.h:262 */
+void assist_init(struct assist_extras* assist, struct reb_simulation* sim, struct assist_ephem* ephem);  /* src/assist.h:265 */
+void assist_free_pointers(struct assist_extras* assist);                                     /* src/assist.h:266 */
+void assist_ephem_free_pointers(struct assist_ephem* ephem);                                 /* src/assist.h:267 */
+struct assist_ephem* assist_ephem_create(char* planets_file_name, char* asteroids_file_name);  /* src/assist.h:274 */
+int assist_ephem_init(struct assist_ephem* ephem, char* user_planets_path, char* user_asteroids_path);  /* src/assist.h:290 */
+
+/* REBOUND's additional_forces callback, src/forces.h / src/forces.c:49.
+ * Reads sim->particles (host), evaluates ephemeris + forces + variational
+ * partials on the device and adds the accelerations into sim->particles[].a*
+ * exactly as the CPU callback does (REBOUND zeroes them before the call). */
+void assist_additional_forces(struct reb_simulation* sim);
+
+/* Body state at time t, src/forces.h / src/forces.c:175.  `ephem_cache` is
+ * accepted for signature compatibility and ignored. */
+int assist_all_ephem(const struct assist_ephem* ephem, struct assist_ephem_cache* ephem_cache,
+                     const int i, const double t, double* const GM,
+                     double* const x, double* const y, double* const z,
+                     double* const vx, double* const vy, double* const vz,
+                     double* const ax, double* const ay, double* const az);
+
+/* ------------------------------------------------------------------------
+ * Batched device API (no ASSIST counterpart: ASSIST integrates one REBOUND
+ * simulation at a time on one CPU core).
+ * ---------------------------------------------------------------------- */
+
+/* Options shared by the batched entry points.  Force-model fields mean what
+ * the assist_extras fields of the same name mean (src/assist.h:177-195). */
+struct assist_gb300_options {
+    int forces;             /* ASSIST_FORCES bits (ASSIST default 0x7F) */
+    int gr_eih_sources;     /* EIH source bodies, ASSIST default 1 */
+    int geocentric;         /* 0 barycentric (default), 1 geocentric */
+    double alpha, nk, nm, nn, r0;   /* Marsden g(r) law, ASSIST defaults 1,0,2,5.093,1 */
+    double epsilon;         /* IAS15 tolerance (1e-9); 0 => fixed step = dt0 */
+    double min_dt;          /* IAS15 minimum |dt| (0 => none) */
+    double dt0;             /* initial |dt| (REBOUND default 0.001 day) */
+    int max_steps;          /* per-particle step budget, 0 => unlimited */
+    int warm_start;         /* 0 plain predictor, 1 learned warm start (needs a loaded MLP) */
+    int threads_per_block;  /* 0 => autotuned */
+};
+
+/* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */
+void assist_gb300_default_options(struct assist_gb300_options* opt);
+
+/* Per-particle result status word of the batched integrator. */
+enum ASSIST_GB300_PARTICLE_STATUS {
+    ASSIST_GB300_OK = 0,
+    ASSIST_GB300_COVERAGE = 1,      /* a substep time fell outside the ephemeris */
+    ASSIST_GB300_NONFINITE = 2,     /* NaN/Inf in state or acceleration */
+    ASSIST_GB300_STEP_BUDGET = 3,   /* max_steps reached before t_end */
+    ASSIST_GB300_MIN_DT = 4,        /* informational: min_dt clamp was applied */
+};
+
+/* Statistics returned by the batched integrator. */
+struct assist_gb300_batch_stats {
+    long long steps_accepted;
+    long long steps_rejected;
+    long long force_evals;          /* particle force evaluations (real particles) */
+    long long pc_iterations;        /* predictor-corrector iterations summed over steps */
+    long long warm_start_used;      /* steps whose learned start was accepted */
+    long long warm_start_fallback;  /* steps that fell back to the plain predictor */
+    double kernel_ms;               /* device time of the integration kernels */
+};
+
+/* Integrate n independent test particles, each from t0[i] to t_end[i] (days
+ * relative to ephem->jd_ref) with its own adaptive IAS15 step.
+ *   state  : host array n*6 doubles (x,y,z,vx,vy,vz), overwritten with the end state
+ *   params : host array n*3 (A1,A2,A3 non-grav) or NULL
+ *   n_var  : 0 or 6; with 6, `var_state` holds n*6*6 doubles (6 first-order
+ *            variational states per particle) and is overwritten at the end
+ *   status : host array n ints (ASSIST_GB300_PARTICLE_STATUS), may be NULL
+ * Returns ASSIST_SUCCESS or an ASSIST_STATUS error. */
+int assist_gb300_integrate_batch(const struct assist_ephem* ephem, const struct assist_gb300_options* opt,
+                                 int n, const double* t0, const double* t_end,
+                                 double* state, const double* params,
+                                 int n_var, double* var_state,
+                                 int* status, struct assist_gb300_batch_stats* stats);
+
+/* Same as assist_gb300_integrate_batch but every array is a DEVICE pointer on
+ * the current CUDA device and the call is asynchronous on `stream`
+ * (cudaStream_t passed as void*).  `stats` (host) is filled after an internal
+ * stream synchronisation when non-NULL. */
+int assist_gb300_integrate_batch_device(const struct assist_ephem* ephem, const struct assist_gb300_options* opt,
+                                        int n, const double* d_t0, const double* d_t_end,
+                                        double* d_state, const double* d_params,
+                                        int n_var, double* d_var_state,
+                                        int* d_status, void* stream,
+                                        struct assist_gb300_batch_stats* stats);
+
+/* One force evaluation for n particles at per-particle times t[i] (device
+ * pointers): acc[3i..3i+2] = a(x_i, v_i, t_i) for the force model in `opt`.
+ * With n_var = 6, var_state holds per-particle 6 variational states (6 doubles
+ * each) and var_acc receives their accelerations.  status (device, may be NULL)
+ * receives per-particle ASSIST_STATUS codes. */
+int assist_gb300_forces_device(const struct assist_ephem* ephem, const struct assist_gb300_options* opt,
+                               int n, const double* d_t, const double* d_state, const double* d_params,
+                               int n_var, const double* d_var_state,
+                               double* d_acc, double* d_var_acc, int* d_status, void* stream);
+
+/* Evaluate all 11+N_ast bodies at n times (device pointers).  out holds, per
+ * time, (11+N_ast) records of 10 doubles: GM, x,y,z, vx,vy,vz, ax,ay,az, with
+ * the same meaning as assist_all_ephem (asteroid velocity/acceleration NaN).
+ * status (device, may be NULL) receives an ASSIST_STATUS per time. */
+int assist_gb300_ephem_device(const struct assist_ephem* ephem, int n, const double* d_t,
+                              double* d_out, int* d_status, void* stream);
+
+/* Number of bodies (11 + asteroids) of a loaded ephemeris. */
+int assist_gb300_n_bodies(const struct assist_ephem* ephem);
+
+/* Last CUDA/library error text of this thread ("" if none). */
+const char* assist_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASSIST_GB300_ASSIST_H */

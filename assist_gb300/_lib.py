@@ -1,0 +1,88 @@
+"""Loader for libassist_gb300.so (mirrors assist/_libassist.py of ASSIST).
+
+The library is built in place by ``assist_gb300.build`` (or
+``__graft_entry__.build()``).  Set ASSIST_GB300_LIB to force a specific file.
+There is no CPU fallback: a missing library is an ImportError.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_void_p
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.environ.get("ASSIST_GB300_LIB", os.path.join(HERE, "libassist_gb300.so"))
+if not os.path.exists(LIBPATH):
+    raise ImportError("libassist_gb300.so not found at %s: run `python -m assist_gb300.build` "
+                      "(or __graft_entry__.build()) first" % LIBPATH)
+clib = ctypes.CDLL(LIBPATH)
+__libpath__ = LIBPATH
+
+
+def _s(name: str) -> str:
+    return c_char_p.in_dll(clib, name).value.decode("ascii")
+
+
+__version__ = _s("assist_version_str")
+__build__ = _s("assist_build_str")
+__githash__ = _s("assist_githash_str")
+
+
+def assist_error_messages(e: int) -> str:
+    n = c_int.in_dll(clib, "assist_error_messages_N").value
+    if e >= n:
+        raise RuntimeError("An error occured while trying to process an ASSIST error message.")
+    return (c_char_p * n).in_dll(clib, "assist_error_messages")[e].decode("ascii")
+
+
+D = POINTER(c_double)
+I = POINTER(c_int)
+
+
+class Options(ctypes.Structure):
+    """struct assist_gb300_options (include/assist.h)."""
+    _fields_ = [("forces", c_int), ("gr_eih_sources", c_int), ("geocentric", c_int),
+                ("alpha", c_double), ("nk", c_double), ("nm", c_double), ("nn", c_double), ("r0", c_double),
+                ("epsilon", c_double), ("min_dt", c_double), ("dt0", c_double), ("max_steps", c_int),
+                ("warm_start", c_int), ("threads_per_block", c_int)]
+
+
+class BatchStats(ctypes.Structure):
+    """struct assist_gb300_batch_stats (include/assist.h)."""
+    _fields_ = [("steps_accepted", c_longlong), ("steps_rejected", c_longlong), ("force_evals", c_longlong),
+                ("pc_iterations", c_longlong), ("warm_start_used", c_longlong), ("warm_start_fallback", c_longlong),
+                ("kernel_ms", c_double)]
+
+
+clib.assist_gb300_default_options.argtypes = [POINTER(Options)]
+clib.assist_gb300_default_options.restype = None
+clib.assist_gb300_integrate_batch.argtypes = [c_void_p, POINTER(Options), c_int, D, D, D, D, c_int, D, I,
+                                              POINTER(BatchStats)]
+clib.assist_gb300_integrate_batch.restype = c_int
+clib.assist_gb300_integrate_batch_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p,
+                                                     c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
+clib.assist_gb300_integrate_batch_device.restype = c_int
+clib.assist_gb300_forces_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p, c_int,
+                                            c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+clib.assist_gb300_forces_device.restype = c_int
+clib.assist_gb300_ephem_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
+clib.assist_gb300_ephem_device.restype = c_int
+clib.assist_gb300_n_bodies.argtypes = [c_void_p]
+clib.assist_gb300_n_bodies.restype = c_int
+clib.assist_gb300_last_error.restype = c_char_p
+clib.assist_gb300_fp64_peak_gflops.restype = c_double
+clib.assist_ephem_create.restype = c_void_p
+clib.assist_ephem_create.argtypes = [c_char_p, c_char_p]
+clib.assist_ephem_free.argtypes = [c_void_p]
+clib.assist_ephem_init.restype = c_int
+clib.assist_detect_ephemeris_file_format.argtypes = [c_int]
+clib.assist_detect_ephemeris_file_format.restype = c_int
+clib.assist_detect_ascii_bin_signature.argtypes = [c_int]
+clib.assist_detect_ascii_bin_signature.restype = c_int
+clib.assist_discover_planets_path.argtypes = [c_char_p, ctypes.c_size_t, c_char_p]
+clib.assist_discover_planets_path.restype = c_int
+
+
+def last_error() -> str:
+    v = clib.assist_gb300_last_error()
+    return v.decode() if v else ""

@@ -1,0 +1,115 @@
+"""Batched device API: many independent particles, each with its own time,
+adaptive IAS15 step and integration length (no ASSIST counterpart: ASSIST
+integrates one REBOUND simulation at a time on one CPU core).
+
+Host-array entry points take numpy arrays; ``*_device`` entry points take
+torch CUDA tensors (torch is used only for device memory and streams).
+"""
+from __future__ import annotations
+
+from ctypes import byref, c_void_p
+from typing import Optional
+
+import numpy as np
+
+from ._lib import BatchStats, D, I, Options, clib, last_error
+from .ephem import Ephem
+
+
+def options(**kw) -> Options:
+    """ASSIST's defaults (src/assist.c:408-447) overridden by keyword arguments:
+    forces, gr_eih_sources, geocentric, alpha, nk, nm, nn, r0, epsilon, min_dt,
+    dt0, max_steps, warm_start, threads_per_block."""
+    o = Options()
+    clib.assist_gb300_default_options(byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError("unknown option %r" % k)
+        setattr(o, k, v)
+    return o
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(D)
+
+
+def integrate_batch(ephem: Ephem, t0, t_end, state, params=None, var_state=None, opts: Optional[Options] = None):
+    """Integrate n independent particles (state: (n, 6) barycentric AU, AU/day)
+    from t0[i] to t_end[i] (days relative to ephem.jd_ref).  var_state, if
+    given, is (n, 6, 6): six first-order variational states per particle.
+    Returns (state_out, var_out, status, stats_dict)."""
+    o = opts or options()
+    st = np.ascontiguousarray(state, dtype=np.float64).reshape(-1, 6).copy()
+    n = st.shape[0]
+    t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,))).copy()
+    te = np.ascontiguousarray(np.broadcast_to(np.asarray(t_end, np.float64), (n,))).copy()
+    prm = None if params is None else np.ascontiguousarray(params, dtype=np.float64).reshape(n, 3).copy()
+    nv = 0
+    var = None
+    if var_state is not None:
+        var = np.ascontiguousarray(var_state, dtype=np.float64).reshape(n, 6, 6).copy()
+        nv = 6
+    status = np.zeros(n, dtype=np.int32)
+    stats = BatchStats()
+    rc = clib.assist_gb300_integrate_batch(byref(ephem), byref(o), n, _p(t0), _p(te), _p(st), _p(prm), nv,
+                                           _p(var), status.ctypes.data_as(I), byref(stats))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_integrate_batch failed (%d): %s" % (rc, last_error()))
+    return st, var, status, {f: getattr(stats, f) for f, _ in BatchStats._fields_}
+
+
+def _ptr(t):
+    return None if t is None else c_void_p(t.data_ptr())
+
+
+def integrate_batch_device(ephem: Ephem, t0, t_end, state, params=None, var_state=None, status=None,
+                           opts: Optional[Options] = None, stream=None):
+    """Device-resident variant: torch CUDA float64 tensors, state overwritten in place."""
+    o = opts or options()
+    n = state.shape[0]
+    nv = 0 if var_state is None else 6
+    stats = BatchStats()
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_integrate_batch_device(byref(ephem), byref(o), n, _ptr(t0), _ptr(t_end), _ptr(state),
+                                                  _ptr(params), nv, _ptr(var_state), _ptr(status), s, byref(stats))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_integrate_batch_device failed (%d): %s" % (rc, last_error()))
+    return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
+
+
+def forces_device(ephem: Ephem, t, state, params=None, var_state=None, acc=None, var_acc=None, status=None,
+                  opts: Optional[Options] = None, stream=None):
+    """One force evaluation of n particles at their own times t[i] (torch CUDA tensors)."""
+    import torch
+    o = opts or options()
+    n = state.shape[0]
+    if acc is None:
+        acc = torch.empty((n, 3), dtype=torch.float64, device=state.device)
+    nv = 0 if var_state is None else 6
+    if nv and var_acc is None:
+        var_acc = torch.empty((n, 6, 3), dtype=torch.float64, device=state.device)
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_forces_device(byref(ephem), byref(o), n, _ptr(t), _ptr(state), _ptr(params), nv,
+                                         _ptr(var_state), _ptr(acc), _ptr(var_acc), _ptr(status), s)
+    if rc != 0:
+        raise RuntimeError("assist_gb300_forces_device failed (%d): %s" % (rc, last_error()))
+    return acc, var_acc
+
+
+def bodies_device(ephem: Ephem, t, out=None, status=None, stream=None):
+    """All bodies at n times: (n, n_bodies, 10) = GM, x, v, a (torch CUDA)."""
+    import torch
+    n = t.shape[0]
+    nb = clib.assist_gb300_n_bodies(byref(ephem))
+    if out is None:
+        out = torch.empty((n, nb, 10), dtype=torch.float64, device=t.device)
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_ephem_device(byref(ephem), n, _ptr(t), _ptr(out), _ptr(status), s)
+    if rc != 0:
+        raise RuntimeError("assist_gb300_ephem_device failed (%d): %s" % (rc, last_error()))
+    return out
+
+
+def fp64_peak_gflops() -> float:
+    """Measured FP64 FMA throughput of the current device (GFLOP/s)."""
+    return float(clib.assist_gb300_fp64_peak_gflops())

@@ -1,0 +1,696 @@
+/*
+ * api.cpp -- the C ABI: ASSIST's plugin surface (src/assist.h), the REBOUND
+ * subset it is driven through, and the batched entry points.
+ *
+ * Every compute call goes to the device; a missing or failing CUDA device is
+ * reported as an error (ASSIST status / sim->status / return code), never
+ * answered on the CPU.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/assist.h"
+#include "device_forces.cuh"
+#include "internal.h"
+#include "shared_sim.h"
+
+#define AG_STR2(s) #s
+#define AG_STR(s) AG_STR2(s)
+#ifndef ASSIST_GB300_GITHASH
+#define ASSIST_GB300_GITHASH notavailable
+#endif
+
+extern "C" {
+const char* assist_build_str = __DATE__ " " __TIME__;
+const char* assist_version_str = "1.2.0";
+const char* assist_githash_str = AG_STR(ASSIST_GB300_GITHASH);
+const char* assist_error_messages[] = {
+    "No error has occured.",
+    "The JPL planet ephemeris file has not been found.",
+    "The JPL asteroid ephemeris file has not been found. Asteroid forces have been disabled.",
+    "The requested asteroid ID has not been found.",
+    "The requested planet ID has not been found.",
+    "The requested time is outside the coverage provided by the ephemeris file.",
+};
+const int assist_error_messages_N = ASSIST_ERROR_N;
+}
+
+int ag_ephem_device(const struct assist_ephem* e, DevEphem* out);
+int ag_ephem_n_bodies(const struct assist_ephem* e);
+
+/* ---------------------------------------------------------------- errors */
+static thread_local std::string g_last_error;
+void ag_set_error(const std::string& msg) { g_last_error = msg; }
+int ag_cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    ag_set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    std::fprintf(stderr, "(ASSIST gb300) %s: %s\n", what, cudaGetErrorString(e));
+    return 1;
+}
+extern "C" const char* assist_gb300_last_error(void) { return g_last_error.c_str(); }
+
+/* ---------------------------------------------------------------- force config */
+static ForceCfg make_cfg(int forces, int gr, int geo, double alpha, double nk, double nm, double nn, double r0) {
+    ForceCfg c;
+    std::memset(&c, 0, sizeof(c));
+    c.forces = forces;
+    c.gr_eih_sources = gr < 0 ? 0 : (gr > ASSIST_BODY_NPLANETS ? ASSIST_BODY_NPLANETS : gr);
+    c.geocentric = geo;
+    c.alpha = alpha; c.nk = nk; c.nm = nm; c.nn = nn; c.r0 = r0;
+    c.nongrav_rm2 = (nm == 2.0 && nk == 0.0) ? 1 : 0;
+    /* pole directions exactly as ASSIST forms them (src/forces.c:484-490, 670-676) */
+    const double rae = 0.0 * M_PI / 180., dece = 90.0 * M_PI / 180.;
+    c.e_ca = std::cos(rae); c.e_sa = std::sin(rae); c.e_cd = std::cos(dece); c.e_sd = std::sin(dece);
+    const double ras = 286.13 * M_PI / 180., decs = 63.87 * M_PI / 180.;
+    c.s_ca = std::cos(ras); c.s_sa = std::sin(ras); c.s_cd = std::cos(decs); c.s_sd = std::sin(decs);
+    return c;
+}
+static ForceCfg cfg_of(const struct assist_extras* ax) {
+    return make_cfg(ax->forces, ax->gr_eih_sources, ax->geocentric, ax->alpha, ax->nk, ax->nm, ax->nn, ax->r0);
+}
+
+/* ---------------------------------------------------------------- bodies */
+struct BodyScratch {
+    double* d_t = nullptr;
+    double* d_out = nullptr;
+    int* d_st = nullptr;
+    int cap = 0;
+};
+static std::mutex g_body_mu;
+static BodyScratch g_body;
+
+extern "C" int ag_bodies_at(const struct assist_ephem* e, double t, double* out_all) {
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    const int nb = ag_ephem_n_bodies(e);
+    std::lock_guard<std::mutex> lk(g_body_mu);
+    if (g_body.cap < nb) {
+        if (g_body.d_out) cudaFree(g_body.d_out);
+        if (!g_body.d_t && ag_cuda_check(cudaMalloc(&g_body.d_t, sizeof(double)), "cudaMalloc")) return ASSIST_ERROR_EPHEM_FILE;
+        if (!g_body.d_st && ag_cuda_check(cudaMalloc(&g_body.d_st, sizeof(int)), "cudaMalloc")) return ASSIST_ERROR_EPHEM_FILE;
+        if (ag_cuda_check(cudaMalloc(&g_body.d_out, sizeof(double) * 10 * nb), "cudaMalloc")) return ASSIST_ERROR_EPHEM_FILE;
+        g_body.cap = nb;
+    }
+    cudaMemcpy(g_body.d_t, &t, sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemset(g_body.d_st, 0, sizeof(int));
+    if (ag_cuda_check((cudaError_t)ag_launch_bodies(D, 1, g_body.d_t, g_body.d_out, g_body.d_st, 0), "body kernel"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    int hst = 0;
+    if (ag_cuda_check(cudaMemcpy(out_all, g_body.d_out, sizeof(double) * 10 * nb, cudaMemcpyDeviceToHost), "body kernel") ||
+        ag_cuda_check(cudaMemcpy(&hst, g_body.d_st, sizeof(int), cudaMemcpyDeviceToHost), "body kernel"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    return hst;
+}
+
+extern "C" int assist_all_ephem(const struct assist_ephem* ephem, struct assist_ephem_cache* cache, const int i,
+                                const double t, double* const GM, double* const x, double* const y, double* const z,
+                                double* const vx, double* const vy, double* const vz, double* const ax,
+                                double* const ay, double* const az) {
+    (void)cache;
+    const int nb = ag_ephem_n_bodies(ephem);
+    if (i < 0 || i >= nb) {
+        if (i >= ASSIST_BODY_NPLANETS && !ephem->spk_asteroids) return ASSIST_ERROR_AST_FILE;
+        return i < ASSIST_BODY_NPLANETS ? ASSIST_ERROR_NEPHEM : ASSIST_ERROR_NAST;
+    }
+    std::vector<double> all((size_t)nb * 10);
+    int st = ag_bodies_at(ephem, t, all.data());
+    /* a body's own coverage decides, as the per-body reference call does */
+    const double* o = all.data() + 10 * (size_t)i;
+    *GM = o[0];
+    if (st != ASSIST_SUCCESS) {
+        double tb, te;
+        assist_ephem_time_bounds(ephem, &tb, &te);
+        if (st == ASSIST_ERROR_COVERAGE) return st;
+        return st;
+    }
+    *x = o[1]; *y = o[2]; *z = o[3]; *vx = o[4]; *vy = o[5]; *vz = o[6]; *ax = o[7]; *ay = o[8]; *az = o[9];
+    return ASSIST_SUCCESS;
+}
+
+extern "C" struct reb_particle assist_get_particle_with_error(const struct assist_ephem* ephem, const int id,
+                                                              const double t, int* error) {
+    struct reb_particle p;
+    std::memset(&p, 0, sizeof(p));
+    double GM = 0;
+    *error = assist_all_ephem(ephem, nullptr, id, t, &GM, &p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.ax, &p.ay, &p.az);
+    p.m = GM;
+    return p;
+}
+
+extern "C" struct reb_particle assist_get_particle(const struct assist_ephem* ephem, const int id, const double t) {
+    int error = 0;
+    struct reb_particle p = assist_get_particle_with_error(ephem, id, t, &error);
+    if (error != ASSIST_SUCCESS) {
+        std::fprintf(stderr, "(ASSIST) An error occured while trying to initialize particle from ephemeris data.\n");
+        std::fprintf(stderr, "(ASSIST) %s\n", assist_error_messages[error]);
+    }
+    return p;
+}
+
+/* ---------------------------------------------------------------- extras */
+static std::mutex g_ws_mu;
+static std::map<const void*, AgSharedSim*> g_ws;   /* per assist_extras device workspace */
+
+static AgSharedSim* workspace(const struct assist_extras* ax) {
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    auto it = g_ws.find(ax);
+    if (it != g_ws.end()) return it->second;
+    AgSharedSim* s = ag_shared_create();
+    g_ws[ax] = s;
+    return s;
+}
+static void workspace_free(const struct assist_extras* ax) {
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    auto it = g_ws.find(ax);
+    if (it == g_ws.end()) return;
+    ag_shared_free(it->second);
+    g_ws.erase(it);
+}
+
+static void assist_extras_cleanup(struct reb_simulation* sim) {
+    struct assist_extras* a = (struct assist_extras*)sim->extras;
+    if (a) a->sim = nullptr;
+}
+
+extern "C" void assist_init(struct assist_extras* assist, struct reb_simulation* sim, struct assist_ephem* ephem) {
+    assist->sim = sim;
+    assist->ephem_cache = nullptr;
+    assist->gr_eih_sources = 1;
+    assist->ephem = ephem;
+    assist->particle_params = nullptr;
+    assist->forces = ASSIST_FORCE_SUN | ASSIST_FORCE_PLANETS | ASSIST_FORCE_ASTEROIDS | ASSIST_FORCE_NON_GRAVITATIONAL |
+                     ASSIST_FORCE_EARTH_HARMONICS | ASSIST_FORCE_SUN_HARMONICS | ASSIST_FORCE_GR_EIH;
+    assist->last_state = nullptr;
+    assist->current_state = nullptr;
+    assist->alpha = 1.0;
+    assist->nk = 0.0;
+    assist->nm = 2.0;
+    assist->nn = 5.093;
+    assist->r0 = 1.0;
+    sim->integrator = REB_INTEGRATOR_IAS15;
+    sim->gravity = REB_GRAVITY_NONE;
+    sim->extras = assist;
+    sim->extras_cleanup = assist_extras_cleanup;
+    sim->additional_forces = assist_additional_forces;
+    sim->force_is_velocity_dependent = 1;
+    sim->ri_ias15.adaptive_mode = 1;
+}
+
+extern "C" struct assist_extras* assist_attach(struct reb_simulation* sim, struct assist_ephem* ephem) {
+    if (!sim) {
+        std::fprintf(stderr, "(ASSIST) Error: Simulation pointer passed to assist_attach was NULL.\n");
+        return nullptr;
+    }
+    int own = 0;
+    if (!ephem) {
+        ephem = assist_ephem_create(nullptr, nullptr);
+        if (!ephem) {
+            std::fprintf(stderr, "(ASSIST) Error: Ephemeris pointer passed to assist_attach was NULL. Initialization with default path failed.\n");
+            return nullptr;
+        }
+        own = 1;
+    }
+    struct assist_extras* a = (struct assist_extras*)std::calloc(1, sizeof(*a));
+    assist_init(a, sim, ephem);
+    a->extras_should_free_ephem = own;
+    return a;
+}
+
+extern "C" void assist_detach(struct reb_simulation* sim, struct assist_extras* assist) {
+    if (assist->sim) {
+        sim->extras = nullptr;
+        sim->extras_cleanup = nullptr;
+        sim->additional_forces = nullptr;
+        sim->pre_timestep_modifications = nullptr;
+    }
+    assist->sim = nullptr;
+}
+
+extern "C" void assist_free_pointers(struct assist_extras* assist) {
+    if (assist->sim) {
+        assist_detach(assist->sim, assist);
+        assist->sim = nullptr;
+    }
+    std::free(assist->last_state);
+    assist->last_state = nullptr;
+    std::free(assist->current_state);
+    assist->current_state = nullptr;
+    workspace_free(assist);
+    if (assist->extras_should_free_ephem && assist->ephem) {
+        assist_ephem_free(assist->ephem);
+        assist->ephem = nullptr;
+    }
+}
+
+extern "C" void assist_free(struct assist_extras* assist) {
+    if (!assist) return;
+    assist_free_pointers(assist);
+    std::free(assist);
+}
+
+extern "C" void assist_error(struct assist_extras* assist, const char* const msg) {
+    if (assist->sim == nullptr)
+        std::fprintf(stderr, "(ASSIST) Error: A Simulation is no longer attached to the ASSIST extras instance. Most likely the Simulation has been freed.\n");
+    else
+        reb_simulation_error(assist->sim, msg);
+}
+
+/* REBOUND's additional_forces callback: every particle of the simulation at
+ * sim->t on the device, accelerations added into sim->particles. */
+extern "C" void assist_additional_forces(struct reb_simulation* sim) {
+    struct assist_extras* ax = (struct assist_extras*)sim->extras;
+    if (!ax || !ax->ephem) return;
+    DevEphem D;
+    int st = ag_ephem_device(ax->ephem, &D);
+    if (st != ASSIST_SUCCESS) {
+        reb_simulation_error(sim, assist_error_messages[st]);
+        sim->status = REB_STATUS_GENERIC_ERROR;
+        return;
+    }
+    const ForceCfg c = cfg_of(ax);
+    int fst = 0;
+    if (ag_shared_forces(workspace(ax), D, c, sim, ax->particle_params, &fst)) {
+        reb_simulation_error(sim, ("(ASSIST gb300) device error: " + g_last_error).c_str());
+        sim->status = REB_STATUS_GENERIC_ERROR;
+        return;
+    }
+    if (fst != ASSIST_SUCCESS) {
+        reb_simulation_error(sim, assist_error_messages[fst < ASSIST_ERROR_N ? fst : ASSIST_ERROR_COVERAGE]);
+        sim->status = REB_STATUS_GENERIC_ERROR;
+    }
+}
+
+/* ---------------------------------------------------------------- REBOUND subset */
+extern "C" struct reb_simulation* reb_simulation_create(void) {
+    struct reb_simulation* r = (struct reb_simulation*)std::calloc(1, sizeof(*r));
+    r->G = 1.0;
+    r->dt = 0.001;
+    r->status = REB_STATUS_RUNNING;
+    r->exact_finish_time = 1;
+    r->integrator = REB_INTEGRATOR_IAS15;
+    r->gravity = REB_GRAVITY_BASIC;
+    r->ri_ias15.epsilon = 1e-9;
+    r->ri_ias15.min_dt = 0.0;
+    r->ri_ias15.adaptive_mode = 2;
+    return r;
+}
+
+static void free_dense(struct reb_simulation* r) {
+    std::free(r->ri_ias15.x0); std::free(r->ri_ias15.v0); std::free(r->ri_ias15.a0);
+    std::free(r->ri_ias15.br.p0);
+    r->ri_ias15.x0 = r->ri_ias15.v0 = r->ri_ias15.a0 = nullptr;
+    std::memset(&r->ri_ias15.br, 0, sizeof(r->ri_ias15.br));
+    r->ri_ias15.N_allocated = 0;
+}
+
+extern "C" void reb_simulation_free(struct reb_simulation* r) {
+    if (!r) return;
+    if (r->extras_cleanup) r->extras_cleanup(r);
+    free_dense(r);
+    std::free(r->particles);
+    std::free(r->var_config);
+    std::free(r);
+}
+
+extern "C" void reb_simulation_add(struct reb_simulation* r, struct reb_particle p) {
+    if (r->N >= r->N_allocated) {
+        r->N_allocated = r->N_allocated ? 2 * r->N_allocated : 16;
+        r->particles = (struct reb_particle*)std::realloc(r->particles, sizeof(struct reb_particle) * (size_t)r->N_allocated);
+    }
+    p.sim = r;
+    r->particles[r->N++] = p;
+}
+
+extern "C" int reb_simulation_add_variation_1st_order(struct reb_simulation* r, int testparticle) {
+    if (r->N_var_config >= r->N_allocated_var_config) {
+        r->N_allocated_var_config = r->N_allocated_var_config ? 2 * r->N_allocated_var_config : 8;
+        r->var_config = (struct reb_variational_configuration*)std::realloc(
+            r->var_config, sizeof(struct reb_variational_configuration) * (size_t)r->N_allocated_var_config);
+    }
+    struct reb_variational_configuration* vc = &r->var_config[r->N_var_config++];
+    std::memset(vc, 0, sizeof(*vc));
+    vc->sim = r;
+    vc->order = 1;
+    vc->testparticle = testparticle;
+    vc->index = r->N;
+    vc->index_1st_order_a = -1;
+    vc->index_1st_order_b = -1;
+    vc->lrescale = 0.0;
+    struct reb_particle p;
+    std::memset(&p, 0, sizeof(p));
+    reb_simulation_add(r, p);
+    r->N_var++;
+    return vc->index;
+}
+
+extern "C" void reb_simulation_error(struct reb_simulation* r, const char* msg) {
+    if (!r) return;
+    std::strncpy(r->error_message, msg, sizeof(r->error_message) - 1);
+    r->error_message[sizeof(r->error_message) - 1] = '\0';
+    std::fprintf(stderr, "REBOUND Error: %s\n", msg);
+}
+
+extern "C" void reb_simulation_warning(struct reb_simulation* r, const char* msg) {
+    (void)r;
+    std::fprintf(stderr, "REBOUND Warning: %s\n", msg);
+}
+
+extern "C" void reb_simulation_update_acceleration(struct reb_simulation* r) {
+    for (int i = 0; i < r->N; i++) r->particles[i].ax = r->particles[i].ay = r->particles[i].az = 0.0;
+    if (r->additional_forces) r->additional_forces(r);
+}
+
+static int integrate_device(struct reb_simulation* r, double tmax, long long max_steps, bool dense) {
+    struct assist_extras* ax = (struct assist_extras*)r->extras;
+    if (!ax || !ax->ephem || r->additional_forces != assist_additional_forces) {
+        reb_simulation_error(r, "this REBOUND subset integrates only simulations with ASSIST attached");
+        r->status = REB_STATUS_GENERIC_ERROR;
+        return r->status;
+    }
+    DevEphem D;
+    int st = ag_ephem_device(ax->ephem, &D);
+    if (st) {
+        reb_simulation_error(r, assist_error_messages[st]);
+        r->status = REB_STATUS_GENERIC_ERROR;
+        return r->status;
+    }
+    ShIntegrateOut out;
+    out.max_steps = max_steps;
+    if (dense) {
+        const int n = r->N;
+        if (r->ri_ias15.N_allocated < n) {
+            free_dense(r);
+            r->ri_ias15.x0 = (double*)std::calloc(3 * (size_t)n, sizeof(double));
+            r->ri_ias15.v0 = (double*)std::calloc(3 * (size_t)n, sizeof(double));
+            r->ri_ias15.a0 = (double*)std::calloc(3 * (size_t)n, sizeof(double));
+            double* b = (double*)std::calloc(21 * (size_t)n, sizeof(double));
+            double** pp[7] = {&r->ri_ias15.br.p0, &r->ri_ias15.br.p1, &r->ri_ias15.br.p2, &r->ri_ias15.br.p3,
+                              &r->ri_ias15.br.p4, &r->ri_ias15.br.p5, &r->ri_ias15.br.p6};
+            for (int q = 0; q < 7; q++) *pp[q] = b + (size_t)q * 3 * n;
+            r->ri_ias15.N_allocated = n;
+        }
+        out.dense = true;
+        out.dense_x0 = r->ri_ias15.x0; out.dense_v0 = r->ri_ias15.v0; out.dense_a0 = r->ri_ias15.a0;
+        double* pp[7] = {r->ri_ias15.br.p0, r->ri_ias15.br.p1, r->ri_ias15.br.p2, r->ri_ias15.br.p3,
+                         r->ri_ias15.br.p4, r->ri_ias15.br.p5, r->ri_ias15.br.p6};
+        for (int q = 0; q < 7; q++) out.dense_b[q] = pp[q];
+    }
+    r->status = REB_STATUS_RUNNING;
+    if (ag_shared_integrate(workspace(ax), D, cfg_of(ax), r, ax->particle_params, tmax, &out)) {
+        reb_simulation_error(r, ("(ASSIST gb300) device error: " + g_last_error).c_str());
+        r->status = REB_STATUS_GENERIC_ERROR;
+        return r->status;
+    }
+    r->steps_done += (unsigned long long)out.accepted;
+    ax->steps_done += (int)out.accepted;
+    if (out.dt_last_done != 0.0) r->dt_last_done = out.dt_last_done;
+    if (out.status > 0) {
+        reb_simulation_error(r, assist_error_messages[out.status < ASSIST_ERROR_N ? out.status : ASSIST_ERROR_COVERAGE]);
+        r->status = REB_STATUS_GENERIC_ERROR;
+    } else {
+        r->status = REB_STATUS_SUCCESS;
+    }
+    return r->status;
+}
+
+extern "C" int reb_simulation_integrate(struct reb_simulation* r, double tmax) {
+    return integrate_device(r, tmax, 0, false);
+}
+
+/* One step of size r->dt (possibly retried with a smaller one after a
+ * rejection): integrate to t + dt without forcing the end time. */
+extern "C" void reb_simulation_step(struct reb_simulation* r) {
+    struct assist_extras* ax = (struct assist_extras*)r->extras;
+    (void)ax;
+    integrate_device(r, r->t + r->dt, 1, false);
+}
+
+/* ---------------------------------------------------------------- dense output */
+static void gauss_radau_eval(const double* x0, const double* v0, const double* a0, double* const b[7], double dt,
+                             double h, int N, struct reb_particle* out) {
+    double s[9], sv[8];
+    s[0] = dt * h;
+    s[1] = s[0] * s[0] / 2.;
+    s[2] = s[1] * h / 3.;
+    s[3] = s[2] * h / 2.;
+    s[4] = 3. * s[3] * h / 5.;
+    s[5] = 2. * s[4] * h / 3.;
+    s[6] = 5. * s[5] * h / 7.;
+    s[7] = 3. * s[6] * h / 4.;
+    s[8] = 7. * s[7] * h / 9.;
+    sv[0] = dt * h;
+    for (int k = 1; k < 8; k++) sv[k] = (double)k * sv[k - 1] * h / (double)(k + 1);
+    for (int j = 0; j < N; j++)
+        for (int k = 0; k < 3; k++) {
+            const int q = 3 * j + k;
+            double x = s[8] * b[6][q] + s[7] * b[5][q] + s[6] * b[4][q] + s[5] * b[3][q] + s[4] * b[2][q] + s[3] * b[1][q] +
+                       s[2] * b[0][q] + s[1] * a0[q] + s[0] * v0[q];
+            double v = sv[7] * b[6][q] + sv[6] * b[5][q] + sv[5] * b[4][q] + sv[4] * b[3][q] + sv[3] * b[2][q] +
+                       sv[2] * b[1][q] + sv[1] * b[0][q] + sv[0] * a0[q];
+            (&out[j].x)[k] = x0[q] + x;
+            (&out[j].vx)[k] = v0[q] + v;
+        }
+}
+
+/* src/assist.c:642-680: integrate only when t is outside the last step,
+ * otherwise evaluate the Gauss-Radau polynomial of the last step. */
+extern "C" void assist_integrate_or_interpolate(struct assist_extras* ax, double t) {
+    struct reb_simulation* sim = ax->sim;
+    const int N = sim->N;
+    if (!ax->current_state) {
+        ax->current_state = (struct reb_particle*)std::malloc(sizeof(struct reb_particle) * (size_t)N);
+        ax->last_state = (struct reb_particle*)std::malloc(sizeof(struct reb_particle) * (size_t)N);
+        std::memcpy(ax->current_state, sim->particles, sizeof(struct reb_particle) * (size_t)N);
+        std::memcpy(ax->last_state, sim->particles, sizeof(struct reb_particle) * (size_t)N);
+    } else {
+        struct reb_particle* p = sim->particles;
+        sim->particles = ax->current_state;
+        ax->current_state = p;
+    }
+    const double dts = std::copysign(1., sim->dt_last_done);
+    if (dts * (sim->t - sim->dt_last_done) > dts * t || dts * t > dts * sim->t || sim->dt_last_done == 0.0) {
+        sim->exact_finish_time = 0;
+        /* integrate past t without forcing the end time: steps until t is inside the last step */
+        const double dir = std::copysign(1.0, t - sim->t);
+        while (dir * (t - sim->t) > 0 && sim->status <= 0) {
+            if (sim->dt * dir <= 0) sim->dt = dir * std::fabs(sim->dt);
+            integrate_device(sim, sim->t + sim->dt, 1, true);
+            if (sim->status > 0) break;
+        }
+    }
+    const double h = 1.0 - (sim->t - t) / sim->dt_last_done;
+    if (sim->status > 0) {
+        std::printf("Error: simulation exited with status %d.\n", sim->status);
+    } else if (sim->t - t == 0.) {
+        std::memcpy(ax->current_state, sim->particles, sizeof(struct reb_particle) * (size_t)N);
+    } else if (h < 0.0 || h >= 1.0 || !std::isnormal(h)) {
+        std::printf("Error: cannot interpolate beyond timestep bounds (h=%e).\n", h);
+    } else if (sim->ri_ias15.br.p0 == nullptr) {
+        std::printf("Error: cannot interpolate before first timestep is complete (h=%e).\n", h);
+    } else {
+        double* b[7] = {sim->ri_ias15.br.p0, sim->ri_ias15.br.p1, sim->ri_ias15.br.p2, sim->ri_ias15.br.p3,
+                        sim->ri_ias15.br.p4, sim->ri_ias15.br.p5, sim->ri_ias15.br.p6};
+        std::memcpy(ax->current_state, sim->particles, sizeof(struct reb_particle) * (size_t)N);
+        gauss_radau_eval(sim->ri_ias15.x0, sim->ri_ias15.v0, sim->ri_ias15.a0, b, sim->dt_last_done, h, N,
+                         ax->current_state);
+    }
+    struct reb_particle* p = sim->particles;
+    sim->particles = ax->current_state;
+    ax->current_state = p;
+}
+
+/* src/assist.c:682-752: positions/velocities of sim1 advanced by h of sim2's
+ * last step from sim1's stored start state. */
+extern "C" int assist_interpolate_simulation(struct reb_simulation* sim1, struct reb_simulation* sim2, double h) {
+    if (!sim1->ri_ias15.x0 || !sim2->ri_ias15.br.p0) return 0;
+    double* b[7] = {sim2->ri_ias15.br.p0, sim2->ri_ias15.br.p1, sim2->ri_ias15.br.p2, sim2->ri_ias15.br.p3,
+                    sim2->ri_ias15.br.p4, sim2->ri_ias15.br.p5, sim2->ri_ias15.br.p6};
+    gauss_radau_eval(sim1->ri_ias15.x0, sim1->ri_ias15.v0, sim2->ri_ias15.a0, b, sim2->dt_last_done, h, sim1->N,
+                     sim1->particles);
+    sim1->t += sim2->dt_last_done * h;
+    return 1;
+}
+
+/* ---------------------------------------------------------------- batched API */
+extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->forces = ASSIST_FORCE_SUN | ASSIST_FORCE_PLANETS | ASSIST_FORCE_ASTEROIDS | ASSIST_FORCE_NON_GRAVITATIONAL |
+                ASSIST_FORCE_EARTH_HARMONICS | ASSIST_FORCE_SUN_HARMONICS | ASSIST_FORCE_GR_EIH;
+    o->gr_eih_sources = 1;
+    o->geocentric = 0;
+    o->alpha = 1.0; o->nk = 0.0; o->nm = 2.0; o->nn = 5.093; o->r0 = 1.0;
+    o->epsilon = 1e-9;
+    o->min_dt = 0.0;
+    o->dt0 = 0.001;
+    o->max_steps = 1000000;
+    o->warm_start = 0;
+    o->threads_per_block = 0;
+}
+
+extern "C" int assist_gb300_n_bodies(const struct assist_ephem* e) { return ag_ephem_n_bodies(e); }
+
+extern "C" int assist_gb300_ephem_device(const struct assist_ephem* e, int n, const double* d_t, double* d_out,
+                                         int* d_status, void* stream) {
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    if (d_status) cudaMemsetAsync(d_status, 0, sizeof(int) * (size_t)n, (cudaStream_t)stream);
+    if (ag_cuda_check((cudaError_t)ag_launch_bodies(D, n, d_t, d_out, d_status, (cudaStream_t)stream), "body kernel"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    return ASSIST_SUCCESS;
+}
+
+extern "C" int assist_gb300_forces_device(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                                          const double* d_t, const double* d_state, const double* d_params, int n_var,
+                                          const double* d_var_state, double* d_acc, double* d_var_acc, int* d_status,
+                                          void* stream) {
+    if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    const ForceCfg c = make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
+    if (ag_cuda_check((cudaError_t)ag_launch_forces_each(D, c, n, d_t, d_state, d_params, n_var, d_var_state, d_acc,
+                                                         d_var_acc, d_status, (cudaStream_t)stream), "force kernel"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    return ASSIST_SUCCESS;
+}
+
+struct BatchScratch {
+    int* d_order = nullptr;
+    int* d_queue = nullptr;
+    unsigned long long* d_counters = nullptr;
+    double* d_ws = nullptr;
+    size_t ws_cap = 0;
+    int order_cap = 0;
+};
+static std::mutex g_batch_mu;
+static BatchScratch g_batch;
+
+extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e, const struct assist_gb300_options* o,
+                                                   int n, const double* d_t0, const double* d_t_end, double* d_state,
+                                                   const double* d_params, int n_var, double* d_var_state, int* d_status,
+                                                   void* stream, struct assist_gb300_batch_stats* stats) {
+    if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
+    if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
+    if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    const ForceCfg c = make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
+    cudaStream_t s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    const int tpb = o->threads_per_block > 0 ? o->threads_per_block : 128;
+    int nslots = ag_batch_max_slots(n_var, tpb);
+    if (nslots > n) nslots = n;
+    /* queue order: longest integrations first, so the last particles taken are short */
+    std::vector<double> t0((size_t)n), te((size_t)n);
+    if (ag_cuda_check(cudaMemcpyAsync(t0.data(), d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
+        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end") ||
+        ag_cuda_check(cudaStreamSynchronize(s), "read times"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; i++) order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
+    });
+    if (g_batch.order_cap < n) {
+        if (g_batch.d_order) cudaFree(g_batch.d_order);
+        if (ag_cuda_check(cudaMalloc(&g_batch.d_order, sizeof(int) * (size_t)n), "cudaMalloc(order)")) return ASSIST_ERROR_EPHEM_FILE;
+        g_batch.order_cap = n;
+    }
+    if (!g_batch.d_queue) {
+        if (ag_cuda_check(cudaMalloc(&g_batch.d_queue, sizeof(int)), "cudaMalloc") ||
+            ag_cuda_check(cudaMalloc(&g_batch.d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc"))
+            return ASSIST_ERROR_EPHEM_FILE;
+    }
+    const size_t wsn = ag_batch_ws_doubles(nslots, n_var);
+    if (wsn > g_batch.ws_cap) {
+        if (g_batch.d_ws) cudaFree(g_batch.d_ws);
+        g_batch.d_ws = nullptr;
+        if (ag_cuda_check(cudaMalloc(&g_batch.d_ws, sizeof(double) * wsn), "cudaMalloc(IAS15 slots)")) {
+            g_batch.ws_cap = 0;
+            return ASSIST_ERROR_EPHEM_FILE;
+        }
+        g_batch.ws_cap = wsn;
+    }
+    cudaMemcpyAsync(g_batch.d_order, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(g_batch.d_queue, 0, sizeof(int), s);
+    cudaMemsetAsync(g_batch.d_counters, 0, 8 * sizeof(unsigned long long), s);
+    AgBatchArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = n; a.nslots = nslots; a.order = g_batch.d_order; a.queue = g_batch.d_queue;
+    a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
+    a.status = d_status; a.ws = g_batch.d_ws; a.counters = g_batch.d_counters;
+    a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
+    a.watchdog_cycles = (long long)(600.0 * 2.2e9);    /* ~10 minutes at the boost clock */
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    int le = ag_launch_batch(D, c, a, n_var, tpb, s);
+    cudaEventRecord(e1, s);
+    if (le) { cudaEventDestroy(e0); cudaEventDestroy(e1); ag_cuda_check((cudaError_t)le, "batch kernel launch"); return ASSIST_ERROR_EPHEM_FILE; }
+    if (stats) {
+        unsigned long long cnt[8];
+        cudaMemcpyAsync(cnt, g_batch.d_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s);
+        if (ag_cuda_check(cudaStreamSynchronize(s), "batch kernel")) { cudaEventDestroy(e0); cudaEventDestroy(e1); return ASSIST_ERROR_EPHEM_FILE; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats->steps_accepted = (long long)cnt[0];
+        stats->steps_rejected = (long long)cnt[1];
+        stats->force_evals = (long long)cnt[2];
+        stats->pc_iterations = (long long)cnt[3];
+        stats->warm_start_used = (long long)cnt[4];
+        stats->warm_start_fallback = (long long)cnt[5];
+        stats->kernel_ms = ms;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return ASSIST_SUCCESS;
+}
+
+extern "C" int assist_gb300_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                                            const double* t0, const double* t_end, double* state, const double* params,
+                                            int n_var, double* var_state, int* status,
+                                            struct assist_gb300_batch_stats* stats) {
+    if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
+    double *d_t0 = nullptr, *d_te = nullptr, *d_st = nullptr, *d_p = nullptr, *d_v = nullptr;
+    int* d_s = nullptr;
+    const size_t nv = (size_t)n * (size_t)n_var * 6;
+    bool ok = !ag_cuda_check(cudaMalloc(&d_t0, sizeof(double) * n), "cudaMalloc") &&
+              !ag_cuda_check(cudaMalloc(&d_te, sizeof(double) * n), "cudaMalloc") &&
+              !ag_cuda_check(cudaMalloc(&d_st, sizeof(double) * 6 * (size_t)n), "cudaMalloc") &&
+              !ag_cuda_check(cudaMalloc(&d_s, sizeof(int) * (size_t)n), "cudaMalloc") &&
+              (!params || !ag_cuda_check(cudaMalloc(&d_p, sizeof(double) * 3 * (size_t)n), "cudaMalloc")) &&
+              (!nv || !ag_cuda_check(cudaMalloc(&d_v, sizeof(double) * nv), "cudaMalloc"));
+    int rc = ASSIST_ERROR_EPHEM_FILE;
+    if (ok) {
+        cudaMemcpy(d_t0, t0, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_te, t_end, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_st, state, sizeof(double) * 6 * (size_t)n, cudaMemcpyHostToDevice);
+        if (params) cudaMemcpy(d_p, params, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+        if (nv) cudaMemcpy(d_v, var_state, sizeof(double) * nv, cudaMemcpyHostToDevice);
+        struct assist_gb300_batch_stats st;
+        rc = assist_gb300_integrate_batch_device(e, o, n, d_t0, d_te, d_st, d_p, n_var, d_v, d_s, nullptr, &st);
+        if (rc == ASSIST_SUCCESS) {
+            if (ag_cuda_check(cudaMemcpy(state, d_st, sizeof(double) * 6 * (size_t)n, cudaMemcpyDeviceToHost), "copy back"))
+                rc = ASSIST_ERROR_EPHEM_FILE;
+            if (nv) cudaMemcpy(var_state, d_v, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+            if (status) cudaMemcpy(status, d_s, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+            if (stats) *stats = st;
+        }
+    }
+    cudaFree(d_t0); cudaFree(d_te); cudaFree(d_st); cudaFree(d_s);
+    if (d_p) cudaFree(d_p);
+    if (d_v) cudaFree(d_v);
+    return rc;
+}
+
+/* FP64 FMA throughput of the current device in GFLOP/s (roofline denominator). */
+extern "C" double assist_gb300_fp64_peak_gflops(void) { return ag_fp64_probe_gflops(); }

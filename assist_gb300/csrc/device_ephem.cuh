@@ -1,0 +1,230 @@
+/*
+ * device_ephem.cuh -- Chebyshev ephemeris evaluation on sm_103a.
+ *
+ * Planets come from the .440 records (ASSIST src/ascii_ephem.c:27-65,
+ * 275-384): one 32-day record holds every body's coefficients; a body's
+ * column is split into `niv` sub-intervals of `ncf` coefficients per
+ * component.  Asteroids come from SPK type-2 segments (src/spk.c:405-481):
+ * records [MID, RADIUS, X(P), Y(P), Z(P)] in km, heliocentric.
+ *
+ * The file images live in device memory unchanged.  Time arithmetic on
+ * Julian dates (~2.45e6, where one ulp is 4.7e-10 day) is done with the same
+ * operations in the same order as ASSIST so the selected record and the
+ * normalised time agree bit for bit; only the Chebyshev sums (FMA, reciprocal
+ * scale factors) differ from the reference at the rounding level.
+ */
+#ifndef ASSIST_GB300_DEVICE_EPHEM_CUH
+#define ASSIST_GB300_DEVICE_EPHEM_CUH
+
+#include <cstdint>
+
+#define AG_NPL 11
+#define AG_MAX_AST 32
+#define AG_MAX_BODIES (AG_NPL + AG_MAX_AST)
+#define AG_MAX_NCF 24
+#define AG_MAX_SPK_P 32
+
+enum { AG_OK = 0, AG_ERR_EPHEM_FILE = 1, AG_ERR_AST_FILE = 2, AG_ERR_NAST = 3, AG_ERR_NEPHEM = 4, AG_ERR_COVERAGE = 5 };
+enum { AG_SUN = 0, AG_MER, AG_VEN, AG_EAR, AG_MOO, AG_MAR, AG_JUP, AG_SAT, AG_URA, AG_NEP, AG_PLU };
+/* .440 column indices */
+enum { AG_C_MER = 0, AG_C_VEN, AG_C_EMB, AG_C_MAR, AG_C_JUP, AG_C_SAT, AG_C_URA, AG_C_NEP, AG_C_PLU, AG_C_LUN, AG_C_SUN };
+
+/* One SPK type-2 segment, with the Julian-date conversions ASSIST performs per
+ * call (src/spk.c:432-445) done once on the host with the same operations. */
+struct AgSpkSeg {
+    double init_jd;              /* 2451545 + INIT/86400 */
+    double inv_intlen_days;      /* 86400/INTLEN */
+    long long data_off;          /* 0-based index of the first record's MID in the file */
+    int nrec, R, P;
+    int meta_off;                /* index of the first record in rec_meta */
+};
+
+/* Everything a kernel needs to evaluate bodies; passed by value. */
+struct DevEphem {
+    double jd_ref;
+    /* planets (.440) */
+    const double* pl_data;       /* the whole file as doubles; record k at pl_data + k*pl_rec_len */
+    long long pl_ndbl;           /* doubles in the file */
+    int pl_nrec;                 /* records in the file (header and constants included) */
+    int pl_rec_len;              /* doubles per record */
+    double pl_beg, pl_end, pl_inc, pl_cau, pl_cem;
+    int col_off[13], col_ncf[13], col_niv[13];   /* 0-based offsets within a record */
+    double gm[AG_NPL];
+    double inv_cau;              /* 1/AU[km] */
+    double col_vscale[13];       /* (2*niv/inc/86400) * 86400/AU: d/dtau -> AU/day */
+    int pl_inc_pow2;             /* record length is a power of two: divide by multiplying */
+    double pl_inv_inc;
+    /* asteroids (SPK type 2) */
+    int n_ast;
+    const double* spk;           /* the whole SPK file as doubles */
+    long long spk_ndbl;
+    double ast_beg[AG_MAX_AST], ast_end[AG_MAX_AST], ast_res[AG_MAX_AST], ast_gm[AG_MAX_AST];
+    int ast_nseg[AG_MAX_AST], ast_seg0[AG_MAX_AST];
+    const struct AgSpkSeg* segs; /* per segment, see AgSpkSeg */
+    const double2* rec_meta;     /* per SPK record: (MID as JD, 86400/RADIUS) */
+    /* constants (ASSIST src/assist.c:296-309) */
+    double J2E, J3E, J4E, J2SUN, Re_eq, Rs_eq, c_squared, over_c_squared;
+};
+
+/* Planet record selection shared by all eleven planets at one time
+ * (src/ascii_ephem.c:294-300).  Returns AG_OK or AG_ERR_COVERAGE. */
+__device__ __forceinline__ int ag_planet_record(const DevEphem& E, double t, const double** rec, double* tf) {
+    const double jd = E.jd_ref + t;
+    if (jd < E.pl_beg || jd > E.pl_end) return AG_ERR_COVERAGE;
+    const double num = E.jd_ref + t - E.pl_beg;
+    const uint32_t blk = (uint32_t)(E.pl_inc_pow2 ? num * E.pl_inv_inc : num / E.pl_inc);
+    if ((long long)blk + 2 >= (long long)E.pl_nrec) return AG_ERR_COVERAGE;
+    *rec = E.pl_data + (size_t)(blk + 2) * (size_t)E.pl_rec_len;
+    const double fr = (E.jd_ref - E.pl_beg - (double)blk * E.pl_inc) + t;
+    *tf = E.pl_inc_pow2 ? fr * E.pl_inv_inc : fr / E.pl_inc;
+    return AG_OK;
+}
+
+/* One .440 column: position in km (multiply by inv_cau for AU) and optionally
+ * velocity already in AU/day.  tf is the record fraction in [0,1]. */
+template <bool VEL>
+__device__ __forceinline__ void ag_column(const DevEphem& E, const double* rec, int col, double tf,
+                                          double* u, double* v) {
+    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
+    const double tt = tf * (double)niv;
+    const double fl = floor(tt);
+    int b = (int)tt;
+    if (b >= niv) b = niv - 1;                 /* tf == 1 exactly: stay in the last sub-interval */
+    const double tau = 2.0 * (tt - fl) - 1.0;
+    const double two_tau = 2.0 * tau;
+    const double* P = rec + E.col_off[col] + ncf * 3 * b;
+    /* Chebyshev T_p(tau) and S_p = dT_p/dtau by their three-term recurrences */
+    double T0 = 1.0, T1 = tau, S0 = 0.0, S1 = 1.0;
+    double ux = P[0] + tau * P[1], uy = P[ncf] + tau * P[ncf + 1], uz = P[2 * ncf] + tau * P[2 * ncf + 1];
+    double vx = 0.0, vy = 0.0, vz = 0.0;
+    if (VEL) { vx = P[1]; vy = P[ncf + 1]; vz = P[2 * ncf + 1]; }
+#pragma unroll 4
+    for (int p = 2; p < ncf; p++) {
+        const double T2 = fma(two_tau, T1, -T0);
+        ux = fma(T2, P[p], ux);
+        uy = fma(T2, P[ncf + p], uy);
+        uz = fma(T2, P[2 * ncf + p], uz);
+        if (VEL) {
+            const double S2 = fma(two_tau, S1, fma(2.0, T1, -S0));
+            vx = fma(S2, P[p], vx);
+            vy = fma(S2, P[ncf + p], vy);
+            vz = fma(S2, P[2 * ncf + p], vz);
+            S0 = S1; S1 = S2;
+        }
+        T0 = T1; T1 = T2;
+    }
+    u[0] = ux; u[1] = uy; u[2] = uz;
+    if (VEL) {
+        const double c = E.col_vscale[col];
+        v[0] = vx * c; v[1] = vy * c; v[2] = vz * c;
+    }
+}
+
+/* One .440 column: position, velocity and acceleration (U = d2T/dtau2). */
+__device__ __forceinline__ void ag_column_pva(const DevEphem& E, const double* rec, int col, double tf,
+                                              double* u, double* v, double* w) {
+    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
+    const double tt = tf * (double)niv;
+    const double fl = floor(tt);
+    int b = (int)tt;
+    if (b >= niv) b = niv - 1;
+    const double tau = 2.0 * (tt - fl) - 1.0;
+    const double* P = rec + E.col_off[col] + ncf * 3 * b;
+    double T[AG_MAX_NCF], S[AG_MAX_NCF], U[AG_MAX_NCF];
+    T[0] = 1.0; T[1] = tau; S[0] = 0.0; S[1] = 1.0; U[0] = 0.0; U[1] = 0.0; U[2] = 4.0;
+    for (int p = 2; p < ncf; p++) {
+        T[p] = 2.0 * tau * T[p - 1] - T[p - 2];
+        S[p] = 2.0 * tau * S[p - 1] + 2.0 * T[p - 1] - S[p - 2];
+    }
+    for (int p = 3; p < ncf; p++) U[p] = 2.0 * tau * U[p - 1] + 4.0 * S[p - 1] - U[p - 2];
+    const double c = (double)(niv * 2) / E.pl_inc / 86400.0;
+    for (int m = 0; m < 3; m++) {
+        double su = 0.0, sv = 0.0, sw = 0.0;
+        for (int p = 0; p < ncf; p++) {
+            const double cf = P[m * ncf + p];
+            su = fma(T[p], cf, su);
+            sv = fma(S[p], cf, sv);
+            sw = fma(U[p], cf, sw);
+        }
+        u[m] = su; v[m] = sv * c; w[m] = sw * (c * c);
+    }
+}
+
+/* Column of ASSIST body index (Earth and Moon are handled by the caller). */
+__device__ __forceinline__ int ag_col_of(int body) {
+    switch (body) {
+        case AG_SUN: return AG_C_SUN;
+        case AG_MER: return AG_C_MER;
+        case AG_VEN: return AG_C_VEN;
+        case AG_MAR: return AG_C_MAR;
+        case AG_JUP: return AG_C_JUP;
+        case AG_SAT: return AG_C_SAT;
+        case AG_URA: return AG_C_URA;
+        case AG_NEP: return AG_C_NEP;
+        default: return AG_C_PLU;
+    }
+}
+
+/* Full state of planet `body` (0..10): GM, position, velocity, acceleration
+ * in AU and days, as assist_ascii_calc returns them. */
+__device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out) {
+    const double* rec;
+    double tf;
+    out[0] = E.gm[body];
+    int st = ag_planet_record(E, t, &rec, &tf);
+    if (st != AG_OK) return st;
+    double u[3], v[3], w[3];
+    if (body == AG_EAR || body == AG_MOO) {
+        double eu[3], ev[3], ew[3], lu[3], lv[3], lw[3];
+        ag_column_pva(E, rec, AG_C_EMB, tf, eu, ev, ew);
+        ag_column_pva(E, rec, AG_C_LUN, tf, lu, lv, lw);
+        const double f = body == AG_EAR ? -1.0 / (1.0 + E.pl_cem) : E.pl_cem / (1.0 + E.pl_cem);
+        for (int k = 0; k < 3; k++) { u[k] = eu[k] + lu[k] * f; v[k] = ev[k] + lv[k] * f; w[k] = ew[k] + lw[k] * f; }
+    } else {
+        ag_column_pva(E, rec, ag_col_of(body), tf, u, v, w);
+    }
+    for (int k = 0; k < 3; k++) {
+        out[1 + k] = u[k] / E.pl_cau;
+        out[4 + k] = v[k] / (E.pl_cau / 86400.);
+        out[7 + k] = w[k] / (E.pl_cau / (86400. * 86400.));
+    }
+    return AG_OK;
+}
+
+/* Heliocentric asteroid position (AU) from its SPK type-2 segment
+ * (src/spk.c:428-474): segment n from the target's epoch step, record b,
+ * z = (t - MID)/RADIUS, sum of T_p(z) times the X/Y/Z coefficients, km -> AU
+ * with ASSIST's fixed 149597870.7. */
+__device__ __forceinline__ int ag_asteroid_pos(const DevEphem& E, int m, double t, double* p) {
+    const double jd = E.jd_ref + t;
+    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    int n = 0;
+    if (E.ast_nseg[m] > 1) {
+        n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);
+        if (n >= E.ast_nseg[m]) n = E.ast_nseg[m] - 1;
+    }
+    const AgSpkSeg sg = E.segs[E.ast_seg0[m] + n];
+    int b = (int)(((E.jd_ref - sg.init_jd) + t) * sg.inv_intlen_days);
+    if (b >= sg.nrec) b = sg.nrec - 1;
+    if (b < 0) b = 0;
+    const double2 meta = E.rec_meta[sg.meta_off + b];
+    const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2;
+    const int P = sg.P;
+    const double z = ((E.jd_ref - meta.x) + t) * meta.y;
+    const double two_z = 2.0 * z;
+    double T0 = 1.0, T1 = z;
+    double px = fma(z, X[1], X[0]), py = fma(z, X[P + 1], X[P]), pz = fma(z, X[2 * P + 1], X[2 * P]);
+#pragma unroll 4
+    for (int q = 2; q < P; q++) {
+        const double T2 = fma(two_z, T1, -T0);
+        px = fma(T2, X[q], px);
+        py = fma(T2, X[P + q], py);
+        pz = fma(T2, X[2 * P + q], pz);
+        T0 = T1; T1 = T2;
+    }
+    const double s = 1.0 / 149597870.7;
+    p[0] = px * s; p[1] = py * s; p[2] = pz * s;
+    return AG_OK;
+}
+
+#endif

@@ -1,0 +1,480 @@
+/*
+ * host_ephem.cpp -- ephemeris front door: format detection, discovery, the
+ * .440 and SPK loaders, and the device images the kernels read.
+ *
+ * Behaviour follows ASSIST's front door (src/assist.c:62-377):
+ *   - detection: "DAF/SPK " at offset 0 -> SPK; otherwise plausible 6-byte
+ *     constant names at 0x00FC -> .440/.441 (src/assist.c:66-135);
+ *   - discovery under ASSIST_DIR in the order de441.bsp, de440.bsp,
+ *     linux_m13000p17000.441, linux_p1550p2650.440 (src/assist.c:137-154);
+ *   - .440 header fields, constant table and GM values as read by
+ *     src/ascii_ephem.c:105-252 (EMRAT split of GMB into Earth and Moon);
+ *   - SPK summaries collected per target, segment directories, and the
+ *     asteroid GMs from the .440 "MAnnnn" constants (src/assist.c:311-333).
+ * The parsed files are copied to device memory once; the kernels read the
+ * same words ASSIST reads through its mmap.  Planets from an SPK (.bsp)
+ * file are recognised but not evaluated by this library: the planets file
+ * must be in the .440/.441 layout.
+ */
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fcntl.h>
+#include <string>
+#include <unistd.h>
+#include <vector>
+
+#include "../../include/assist.h"
+#include "internal.h"
+
+/* ------------------------------------------------------------ the objects
+ * behind struct assist_ephem's opaque pointers */
+struct ascii_s {
+    double beg, end, inc, cau, cem;
+    int num, ver;
+    int off[15], ncf[15], niv[15], ncm[15];
+    size_t rec;                          /* doubles per record */
+    std::vector<double> data;            /* the file as doubles */
+    std::vector<std::string> names;
+    std::vector<double> con;
+    double mass[ASSIST_BODY_NPLANETS];
+    double J2E, J3E, J4E, J2SUN, AU, RE, CLIGHT, ASUN;
+    double* d_data = nullptr;
+    bool find(const char* name, double* out) const {
+        char key[7] = "      ";
+        for (int i = 0; i < 6 && name[i]; i++) key[i] = name[i];
+        for (size_t p = 0; p < names.size(); p++)
+            if (std::memcmp(names[p].data(), key, 6) == 0) { *out = con[p]; return true; }
+        *out = 0.0;
+        return false;
+    }
+};
+
+struct spk_target_h {
+    int code, cen;
+    double mass, beg, end, res;
+    std::vector<int> one, two;
+};
+struct spk_s {
+    std::vector<spk_target_h> targets;
+    std::vector<double> data;
+    std::vector<AgSpkSeg> segs;
+    std::vector<double2> meta;
+    std::vector<int> seg0;
+    double* d_data = nullptr;
+    AgSpkSeg* d_segs = nullptr;
+    double2* d_meta = nullptr;
+};
+
+static bool read_file(const char* path, std::vector<unsigned char>& out) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    std::fseek(f, 0, SEEK_END);
+    long n = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    if (n <= 0) { std::fclose(f); return false; }
+    out.resize((size_t)n);
+    size_t got = std::fread(out.data(), 1, (size_t)n, f);
+    std::fclose(f);
+    return got == (size_t)n;
+}
+template <class X> static X get(const std::vector<unsigned char>& b, size_t off) {
+    X x;
+    std::memcpy(&x, b.data() + off, sizeof(X));
+    return x;
+}
+
+/* ---------------------------------------------------------------- detection */
+extern "C" int assist_detect_ascii_bin_signature(int fd) {
+    char names[18];
+    if (lseek(fd, 0x00FC, SEEK_SET) != 0x00FC) return 0;
+    if (read(fd, names, sizeof(names)) != (ssize_t)sizeof(names)) return 0;
+    int valid = 0;
+    for (int i = 0; i < 3; i++) {
+        const unsigned char* nm = (const unsigned char*)names + 6 * i;
+        const bool alpha0 = (nm[0] >= 'A' && nm[0] <= 'Z') || (nm[0] >= 'a' && nm[0] <= 'z');
+        if (!alpha0) continue;
+        int alnum = 0;
+        bool ok = true;
+        for (int j = 0; j < 6; j++) {
+            const unsigned char ch = nm[j];
+            if ((ch >= 'A' && ch <= 'Z') || (ch >= 'a' && ch <= 'z') || (ch >= '0' && ch <= '9')) alnum++;
+            else if (ch == ' ' || ch == '\0') { /* padding */ }
+            else { ok = false; break; }
+        }
+        if (ok && alnum >= 2) valid++;
+    }
+    return valid >= 2;
+}
+
+extern "C" ephemeris_file_format_t assist_detect_ephemeris_file_format(int fd) {
+    char buf[1024];
+    lseek(fd, 0, SEEK_SET);
+    ssize_t n = read(fd, buf, sizeof(buf));
+    if (n <= 0) return FILE_FORMAT_UNKNOWN;
+    if (n >= 8 && std::strncmp(buf, "DAF/SPK ", 8) == 0) return FILE_FORMAT_VALID_BSP;
+    if (assist_detect_ascii_bin_signature(fd)) {
+        lseek(fd, 0, SEEK_SET);
+        return FILE_FORMAT_ASCII_BIN;
+    }
+    return FILE_FORMAT_UNKNOWN;
+}
+
+extern "C" int assist_discover_planets_path(char* out_path, size_t out_size, const char* assist_dir) {
+    if (!out_path || out_size == 0 || !assist_dir) return 0;
+    static const char* cand[] = {"/data/de441.bsp", "/data/de440.bsp", "/data/linux_m13000p17000.441",
+                                 "/data/linux_p1550p2650.440"};
+    for (const char* c : cand) {
+        std::snprintf(out_path, out_size, "%s%s", assist_dir, c);
+        if (access(out_path, R_OK) == 0) return 1;
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------- loaders */
+static ascii_s* ascii_load(const char* path) {
+    std::vector<unsigned char> b;
+    if (!read_file(path, b) || b.size() < 0x0B28 + 24) return nullptr;
+    ascii_s* a = new ascii_s();
+    size_t o = 0x0A5C;
+    a->beg = get<double>(b, o); a->end = get<double>(b, o + 8); a->inc = get<double>(b, o + 16);
+    a->num = get<int32_t>(b, o + 24); a->cau = get<double>(b, o + 28); a->cem = get<double>(b, o + 36);
+    o += 44;
+    for (int p = 0; p < 15; p++) a->ncm[p] = 3;
+    a->ncm[11] = 2; a->ncm[14] = 1;
+    for (int p = 0; p < 12; p++, o += 12) {
+        a->off[p] = get<int32_t>(b, o); a->ncf[p] = get<int32_t>(b, o + 4); a->niv[p] = get<int32_t>(b, o + 8);
+    }
+    a->ver = get<int32_t>(b, o); o += 4;
+    a->off[12] = get<int32_t>(b, o); a->ncf[12] = get<int32_t>(b, o + 4); a->niv[12] = get<int32_t>(b, o + 8);
+    if (a->num < 0 || a->num > 100000 || !(a->inc > 0)) { delete a; return nullptr; }
+    size_t tail = 0x0B28 + 6 * (size_t)(a->num > 400 ? a->num - 400 : 0);
+    if (tail + 24 > b.size()) { delete a; return nullptr; }
+    for (int p = 0; p < a->num; p++) {
+        size_t no = p < 400 ? 0x00FC + 6 * (size_t)p : 0x0B28 + 6 * (size_t)(p - 400);
+        a->names.emplace_back((const char*)b.data() + no, 6);
+    }
+    o = tail;
+    for (int p = 13; p < 15; p++, o += 12) {
+        a->off[p] = get<int32_t>(b, o); a->ncf[p] = get<int32_t>(b, o + 4); a->niv[p] = get<int32_t>(b, o + 8);
+    }
+    size_t rec = 2;
+    for (int p = 0; p < 15; p++) {
+        a->off[p] -= 1;
+        if (a->ncf[p] < 0 || a->niv[p] < 0 || a->ncf[p] > AG_MAX_NCF) { delete a; return nullptr; }
+        rec += (size_t)a->ncf[p] * a->niv[p] * a->ncm[p];
+    }
+    a->rec = rec;
+    if (b.size() < 2 * rec * 8) { delete a; return nullptr; }
+    for (int p = 0; p < 11; p++)
+        if (a->off[p] < 2 || (size_t)a->off[p] + (size_t)a->ncf[p] * a->niv[p] * 3 > rec || a->ncf[p] < 2 || a->niv[p] < 1) {
+            delete a; return nullptr;
+        }
+    a->data.resize(b.size() / 8);
+    std::memcpy(a->data.data(), b.data(), a->data.size() * 8);
+    for (int p = 0; p < a->num; p++) a->con.push_back(get<double>(b, rec * 8 + 8 * (size_t)p));
+    double emrat = 0, gmb = 0;
+    a->find("GMS", &a->mass[ASSIST_BODY_SUN]); a->find("GM1", &a->mass[ASSIST_BODY_MERCURY]);
+    a->find("GM2", &a->mass[ASSIST_BODY_VENUS]);
+    a->find("EMRAT", &emrat); a->find("GMB", &gmb);
+    a->mass[ASSIST_BODY_EARTH] = (emrat / (1. + emrat)) * gmb;
+    a->mass[ASSIST_BODY_MOON] = 1. / (1 + emrat) * gmb;
+    a->find("GM4", &a->mass[ASSIST_BODY_MARS]); a->find("GM5", &a->mass[ASSIST_BODY_JUPITER]);
+    a->find("GM6", &a->mass[ASSIST_BODY_SATURN]); a->find("GM7", &a->mass[ASSIST_BODY_URANUS]);
+    a->find("GM8", &a->mass[ASSIST_BODY_NEPTUNE]); a->find("GM9", &a->mass[ASSIST_BODY_PLUTO]);
+    a->find("J2E", &a->J2E); a->find("J3E", &a->J3E); a->find("J4E", &a->J4E); a->find("J2SUN", &a->J2SUN);
+    a->find("AU", &a->AU); a->find("RE", &a->RE); a->find("CLIGHT", &a->CLIGHT); a->find("ASUN", &a->ASUN);
+    if (ag_cuda_check(cudaMalloc(&a->d_data, a->data.size() * 8), "cudaMalloc(.440 records)") ||
+        ag_cuda_check(cudaMemcpy(a->d_data, a->data.data(), a->data.size() * 8, cudaMemcpyHostToDevice), "upload .440")) {
+        if (a->d_data) cudaFree(a->d_data);
+        delete a;
+        return nullptr;
+    }
+    return a;
+}
+
+static void ascii_free(ascii_s* a) {
+    if (!a) return;
+    if (a->d_data) cudaFree(a->d_data);
+    delete a;
+}
+
+static spk_s* spk_load(const char* path) {
+    std::vector<unsigned char> b;
+    if (!read_file(path, b) || b.size() < 1024) return nullptr;
+    if (std::strncmp((const char*)b.data(), "DAF/SPK", 7) != 0) return nullptr;
+    const int nd = get<int32_t>(b, 8), ni = get<int32_t>(b, 12);
+    if (8 * (nd + (ni + 1) / 2) != 40) return nullptr;
+    const int fward = get<int32_t>(b, 76);
+    spk_s* s = new spk_s();
+    long recno = fward;
+    int guard = 0;
+    while (recno > 0 && guard++ < 1000000) {
+        const size_t ro = (size_t)(recno - 1) * 1024;
+        if (ro + 1024 > b.size()) { delete s; return nullptr; }
+        if (b[ro + 8] != 0 && s->targets.empty()) { delete s; return nullptr; }
+        const double next = get<double>(b, ro), nsum = get<double>(b, ro + 16);
+        if (!(nsum >= 0 && nsum <= 25)) { delete s; return nullptr; }
+        for (int k = 0; k < (int)nsum; k++) {
+            const size_t so = ro + 24 + 40 * (size_t)k;
+            const double sbeg = get<double>(b, so), send = get<double>(b, so + 8);
+            const int tar = get<int32_t>(b, so + 16), cen = get<int32_t>(b, so + 20);
+            const int one = get<int32_t>(b, so + 32), two = get<int32_t>(b, so + 36);
+            spk_target_h* t = nullptr;
+            for (auto& x : s->targets) if (x.code == tar) { t = &x; break; }
+            if (!t) {
+                spk_target_h nt;
+                nt.code = tar; nt.cen = cen; nt.mass = 0;
+                nt.beg = 2451545.0 + sbeg / 86400.0;
+                nt.res = (2451545.0 + send / 86400.0) - nt.beg;
+                s->targets.push_back(nt);
+                t = &s->targets.back();
+            }
+            t->one.push_back(one);
+            t->two.push_back(two);
+            t->end = 2451545.0 + send / 86400.0;
+        }
+        recno = (long)next;
+    }
+    s->data.resize(b.size() / 8);
+    std::memcpy(s->data.data(), b.data(), s->data.size() * 8);
+    /* segment table with the per-call Julian-date conversions done once */
+    for (auto& t : s->targets) {
+        s->seg0.push_back((int)s->segs.size());
+        for (size_t q = 0; q < t.one.size(); q++) {
+            const long long two = t.two[q], one = t.one[q];
+            if (two < 4 || (size_t)two > s->data.size() || one < 1 || one > two) { delete s; return nullptr; }
+            const double* dir = s->data.data() + (two - 1);
+            AgSpkSeg g;
+            g.R = (int)dir[-1];
+            g.P = (g.R - 2) / 3;
+            g.nrec = (int)dir[0];
+            if (g.R < 5 || g.P > AG_MAX_SPK_P || g.nrec < 1 || (long long)one - 1 + (long long)g.nrec * g.R > two) {
+                delete s; return nullptr;
+            }
+            g.init_jd = 2451545.0 + dir[-3] / 86400.0;
+            g.inv_intlen_days = 1.0 / (dir[-2] / 86400.0);
+            g.data_off = one - 1;
+            g.meta_off = (int)s->meta.size();
+            for (int r = 0; r < g.nrec; r++) {
+                const double* val = s->data.data() + (one - 1) + (size_t)r * g.R;
+                double2 m;
+                m.x = 2451545.0 + val[0] / 86400.0;
+                m.y = 1.0 / (val[1] / 86400.0);
+                s->meta.push_back(m);
+            }
+            s->segs.push_back(g);
+        }
+    }
+    bool ok = !ag_cuda_check(cudaMalloc(&s->d_data, s->data.size() * 8), "cudaMalloc(SPK)") &&
+              !ag_cuda_check(cudaMemcpy(s->d_data, s->data.data(), s->data.size() * 8, cudaMemcpyHostToDevice), "upload SPK") &&
+              !ag_cuda_check(cudaMalloc(&s->d_segs, sizeof(AgSpkSeg) * (s->segs.size() + 1)), "cudaMalloc(SPK segments)") &&
+              !ag_cuda_check(cudaMemcpy(s->d_segs, s->segs.data(), sizeof(AgSpkSeg) * s->segs.size(), cudaMemcpyHostToDevice), "upload segments") &&
+              !ag_cuda_check(cudaMalloc(&s->d_meta, sizeof(double2) * (s->meta.size() + 1)), "cudaMalloc(SPK records)") &&
+              !ag_cuda_check(cudaMemcpy(s->d_meta, s->meta.data(), sizeof(double2) * s->meta.size(), cudaMemcpyHostToDevice), "upload records");
+    if (!ok) {
+        if (s->d_data) cudaFree(s->d_data);
+        if (s->d_segs) cudaFree(s->d_segs);
+        if (s->d_meta) cudaFree(s->d_meta);
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+static void spk_free(spk_s* s) {
+    if (!s) return;
+    if (s->d_data) cudaFree(s->d_data);
+    if (s->d_segs) cudaFree(s->d_segs);
+    if (s->d_meta) cudaFree(s->d_meta);
+    delete s;
+}
+
+/* ---------------------------------------------------------------- device view */
+int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
+    if (!e || !e->ascii_planets) return ASSIST_ERROR_EPHEM_FILE;
+    const ascii_s* a = e->ascii_planets;
+    DevEphem D;
+    std::memset(&D, 0, sizeof(D));
+    D.jd_ref = e->jd_ref;
+    D.pl_data = a->d_data;
+    D.pl_ndbl = (long long)a->data.size();
+    D.pl_rec_len = (int)a->rec;
+    D.pl_nrec = (int)(a->data.size() / a->rec);
+    D.pl_beg = a->beg; D.pl_end = a->end; D.pl_inc = a->inc; D.pl_cau = a->cau; D.pl_cem = a->cem;
+    for (int p = 0; p < 13; p++) {
+        D.col_off[p] = a->off[p]; D.col_ncf[p] = a->ncf[p]; D.col_niv[p] = a->niv[p];
+        D.col_vscale[p] = ((double)(a->niv[p] * 2) / a->inc / 86400.0) * (86400.0 / a->cau);
+    }
+    for (int k = 0; k < ASSIST_BODY_NPLANETS; k++) D.gm[k] = a->mass[k];
+    D.inv_cau = 1.0 / a->cau;
+    const double l2 = std::log2(a->inc);
+    D.pl_inc_pow2 = (a->inc > 0 && std::floor(l2) == l2) ? 1 : 0;
+    D.pl_inv_inc = 1.0 / a->inc;
+    const spk_s* s = e->spk_asteroids;
+    D.n_ast = 0;
+    if (s) {
+        if ((int)s->targets.size() > AG_MAX_AST) return ASSIST_ERROR_NAST;
+        D.n_ast = (int)s->targets.size();
+        D.spk = s->d_data;
+        D.spk_ndbl = (long long)s->data.size();
+        D.segs = s->d_segs;
+        D.rec_meta = s->d_meta;
+        for (int m = 0; m < D.n_ast; m++) {
+            const spk_target_h& t = s->targets[(size_t)m];
+            D.ast_beg[m] = t.beg; D.ast_end[m] = t.end; D.ast_res[m] = t.res; D.ast_gm[m] = t.mass;
+            D.ast_nseg[m] = (int)t.one.size();
+            D.ast_seg0[m] = s->seg0[(size_t)m];
+        }
+    }
+    D.J2E = e->J2E; D.J3E = e->J3E; D.J4E = e->J4E; D.J2SUN = e->J2SUN;
+    D.Re_eq = e->Re_eq; D.Rs_eq = e->Rs_eq; D.c_squared = e->c_squared; D.over_c_squared = e->over_c_squared;
+    *out = D;
+    return ASSIST_SUCCESS;
+}
+
+int ag_ephem_n_bodies(const struct assist_ephem* e) {
+    return ASSIST_BODY_NPLANETS + (e && e->spk_asteroids ? (int)e->spk_asteroids->targets.size() : 0);
+}
+
+/* Body evaluation through the device kernel (used by assist_all_ephem and
+ * as ephem->planets_calc). */
+extern "C" int ag_bodies_at(const struct assist_ephem* e, double t, double* out_all);
+
+static enum ASSIST_STATUS ag_planets_calc(const struct assist_ephem* e, double jd_ref, double jd_rel, int body,
+                                          double* const GM, double* const x, double* const y, double* const z,
+                                          double* const vx, double* const vy, double* const vz, double* const ax,
+                                          double* const ay, double* const az) {
+    (void)jd_ref;
+    if (body < 0 || body >= ASSIST_BODY_NPLANETS) return ASSIST_ERROR_NEPHEM;
+    std::vector<double> all((size_t)ag_ephem_n_bodies(e) * 10);
+    int st = ag_bodies_at(e, jd_rel, all.data());
+    const double* o = all.data() + 10 * body;
+    *GM = o[0]; *x = o[1]; *y = o[2]; *z = o[3]; *vx = o[4]; *vy = o[5]; *vz = o[6]; *ax = o[7]; *ay = o[8]; *az = o[9];
+    if (st != ASSIST_SUCCESS) return (enum ASSIST_STATUS)st;
+    return ASSIST_SUCCESS;
+}
+
+/* ---------------------------------------------------------------- front door */
+extern "C" int assist_ephem_init(struct assist_ephem* ephem, char* user_planets_path, char* user_asteroids_path) {
+    std::memset(ephem, 0, sizeof(*ephem));
+    ephem->jd_ref = 2451545.0;
+    for (int k = 0; k < ASSIST_BODY_NPLANETS; k++) ephem->spk_target_index[k] = -1;
+    ephem->spk_emb_index = -1;
+    const size_t FN = 1024;
+    char planets[FN], asteroids[FN];
+    const char* base = getenv("ASSIST_DIR");
+    if (user_planets_path == nullptr && base == nullptr) return ASSIST_ERROR_EPHEM_FILE;
+    if (user_planets_path == nullptr) {
+        if (!assist_discover_planets_path(planets, FN, base)) std::snprintf(planets, FN, "%s%s", base, "/data/de441.bsp");
+    } else {
+        std::strncpy(planets, user_planets_path, FN - 1);
+        planets[FN - 1] = '\0';
+    }
+    ephemeris_file_format_t fmt = FILE_FORMAT_UNKNOWN;
+    int fd = open(planets, O_RDONLY);
+    if (fd >= 0) { fmt = assist_detect_ephemeris_file_format(fd); close(fd); }
+    bool ast_missing = false;
+    if (user_asteroids_path == nullptr) {
+        if (base == nullptr) ast_missing = true;
+        else std::snprintf(asteroids, FN, "%s%s", base, "/data/sb441-n16.bsp");
+    } else {
+        std::strncpy(asteroids, user_asteroids_path, FN - 1);
+        asteroids[FN - 1] = '\0';
+    }
+    if (!ast_missing) {
+        ephem->spk_asteroids = spk_load(asteroids);
+        if (!ephem->spk_asteroids) ast_missing = true;
+    }
+    if (fmt == FILE_FORMAT_ASCII_BIN) {
+        ephem->ascii_planets = ascii_load(planets);
+        if (!ephem->ascii_planets) {
+            spk_free(ephem->spk_asteroids);
+            ephem->spk_asteroids = nullptr;
+            return ASSIST_ERROR_EPHEM_FILE;
+        }
+        const ascii_s* a = ephem->ascii_planets;
+        ephem->planets_source = FILE_FORMAT_ASCII_BIN;
+        ephem->J2E = a->J2E; ephem->J3E = a->J3E; ephem->J4E = a->J4E; ephem->J2SUN = a->J2SUN;
+        ephem->AU = a->AU; ephem->RE = a->RE; ephem->CLIGHT = a->CLIGHT; ephem->ASUN = a->ASUN;
+        ephem->EMRAT = a->cem;
+        ephem->Re_eq = ephem->RE / ephem->AU;
+        ephem->Rs_eq = ephem->ASUN / ephem->AU;
+        ephem->c_AU_per_day = (ephem->CLIGHT / ephem->AU) * 86400.0;
+        ephem->c_squared = ephem->c_AU_per_day * ephem->c_AU_per_day;
+        ephem->over_c_squared = 1.0 / ephem->c_squared;
+        ephem->planets_calc = ag_planets_calc;
+        if (ephem->spk_asteroids) {
+            for (auto& t : ephem->spk_asteroids->targets) {
+                if (t.code >= 2000000) {
+                    char key[16];
+                    std::snprintf(key, sizeof(key), "MA%04d", t.code - 2000000);
+                    double gm = 0.0;
+                    if (a->find(key, &gm)) t.mass = gm;
+                } else if (t.code == 399) t.mass = a->mass[ASSIST_BODY_EARTH];
+                else if (t.code == 301) t.mass = a->mass[ASSIST_BODY_MOON];
+                else if (t.code == 10) t.mass = a->mass[ASSIST_BODY_SUN];
+            }
+            if ((int)ephem->spk_asteroids->targets.size() > AG_MAX_AST) {
+                std::fprintf(stderr, "(ASSIST) Asteroid file has more than %d targets.\n", AG_MAX_AST);
+                spk_free(ephem->spk_asteroids);
+                ephem->spk_asteroids = nullptr;
+                ast_missing = true;
+            }
+        }
+    } else {
+        spk_free(ephem->spk_asteroids);
+        ephem->spk_asteroids = nullptr;
+        if (fmt == FILE_FORMAT_VALID_BSP)
+            std::fprintf(stderr, "(ASSIST) Error: '%s' is an SPK planets file; this library evaluates planets from .440/.441 files.\n", planets);
+        else
+            std::fprintf(stderr, "(ASSIST) Error: Failed to initialize planets ephemeris from '%s'.\n", planets);
+        return ASSIST_ERROR_EPHEM_FILE;
+    }
+    if (ast_missing) std::fprintf(stderr, "(ASSIST) %s\n", assist_error_messages[ASSIST_ERROR_AST_FILE]);
+    return ASSIST_SUCCESS;
+}
+
+extern "C" void assist_ephem_free_pointers(struct assist_ephem* ephem) {
+    if (!ephem) return;
+    spk_free(ephem->spk_asteroids);
+    ascii_free(ephem->ascii_planets);
+    ephem->spk_asteroids = nullptr;
+    ephem->ascii_planets = nullptr;
+    ephem->spk_planets = nullptr;
+}
+
+extern "C" void assist_ephem_free(struct assist_ephem* ephem) {
+    if (!ephem) return;
+    assist_ephem_free_pointers(ephem);
+    std::free(ephem);
+}
+
+extern "C" struct assist_ephem* assist_ephem_create(char* planets, char* asteroids) {
+    struct assist_ephem* e = (struct assist_ephem*)std::calloc(1, sizeof(struct assist_ephem));
+    int err = assist_ephem_init(e, planets, asteroids);
+    if (err != ASSIST_SUCCESS) {
+        std::fprintf(stderr, "(ASSIST) An error occured while trying to initialize the ephemeris structure.\n");
+        std::fprintf(stderr, "(ASSIST) %s\n", assist_error_messages[err]);
+        assist_ephem_free(e);
+        return nullptr;
+    }
+    return e;
+}
+
+extern "C" void assist_ephem_time_bounds(const struct assist_ephem* ephem, double* t_beg, double* t_end) {
+    if (!ephem) return;
+    double beg = -INFINITY, end = INFINITY;
+    if (ephem->ascii_planets) {
+        if (ephem->ascii_planets->beg > beg) beg = ephem->ascii_planets->beg;
+        if (ephem->ascii_planets->end < end) end = ephem->ascii_planets->end;
+    }
+    if (ephem->spk_asteroids)
+        for (auto& t : ephem->spk_asteroids->targets) {
+            if (t.beg > beg) beg = t.beg;
+            if (t.end < end) end = t.end;
+        }
+    if (t_beg) *t_beg = beg - ephem->jd_ref;
+    if (t_end) *t_end = end - ephem->jd_ref;
+}

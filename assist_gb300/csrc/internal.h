@@ -1,0 +1,68 @@
+/*
+ * internal.h -- host-side declarations shared by the library's translation units.
+ */
+#ifndef ASSIST_GB300_INTERNAL_H
+#define ASSIST_GB300_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "device_ephem.cuh"
+
+struct ForceCfg;
+
+/* Particle I/O of the shared-time force kernel (one REBOUND simulation). */
+struct AgForceIO {
+    int n_real;             /* real particles (slots 0..n_real-1) */
+    int stride;             /* SoA stride of x, v, a (>= particle count) */
+    const double* x;        /* [3][stride] positions of all particles */
+    const double* v;        /* [3][stride] velocities */
+    double* a;              /* [3][stride] accelerations (written) */
+    const double* params;   /* 3*(n_real + n_var_config) Marsden parameters, or null */
+    const int* var_start;   /* n_real+1 offsets into var_index/var_cfg, or null */
+    const int* var_index;   /* particle slot of each variational particle */
+    const int* var_cfg;     /* its var_config index (row n_real + cfg of params) */
+    int* status;            /* one int, atomically max-ed with an ASSIST status */
+};
+
+/* Device-side state of the batched integrator. */
+struct AgBatchArgs {
+    int n;                          /* particles */
+    int nslots;                     /* persistent threads */
+    const int* order;               /* queue order (indices into the particle arrays) */
+    int* queue;                     /* next queue position (atomic) */
+    const double* t0;
+    const double* t_end;
+    double* state;                  /* [n][6], overwritten with the end state */
+    const double* params;           /* [n][3] or null */
+    double* var_state;              /* [n][NV][6] */
+    int* status;                    /* [n] or null */
+    double* ws;                     /* per-slot workspace, see kernels_ias15.cu */
+    unsigned long long* counters;   /* accepted, rejected, evals, iterations, warm used, warm fallback */
+    double epsilon, min_dt, dt0;
+    long long max_steps;
+    long long watchdog_cycles;      /* per-thread clock64 budget; 0 = none */
+};
+
+/* launchers (kernels_forces.cu, kernels_ias15.cu) */
+int ag_launch_forces_table(const DevEphem& E, const ForceCfg& c, double t, const AgForceIO& io, cudaStream_t s);
+int ag_launch_forces_each(const DevEphem& E, const ForceCfg& c, int n, const double* t, const double* state,
+                          const double* params, int nv, const double* var_state, double* acc, double* var_acc,
+                          int* status, cudaStream_t s);
+int ag_launch_bodies(const DevEphem& E, int n, const double* t, double* out, int* status, cudaStream_t s);
+size_t ag_batch_ws_doubles(int nslots, int nv);
+int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int tpb, cudaStream_t s);
+int ag_batch_max_slots(int nv, int tpb);
+double ag_fp64_probe_gflops(void);
+
+/* shared-step device IAS15 (kernels_shared.cu) */
+struct AgSharedSim;
+AgSharedSim* ag_shared_create(void);
+void ag_shared_free(AgSharedSim* s);
+
+/* library error state */
+void ag_set_error(const std::string& msg);
+int ag_cuda_check(cudaError_t e, const char* what);
+
+#endif

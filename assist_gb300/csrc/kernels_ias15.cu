@@ -1,0 +1,469 @@
+/*
+ * kernels_ias15.cu -- K4: batched, persistent IAS15 with a device work queue.
+ *
+ * Every thread owns one slot.  It takes particle indices from an atomic queue
+ * (ordered longest integration first by the host), integrates that particle
+ * (and its NV first-order variational particles) from t0 to t_end with its own
+ * adaptive IAS15 step, writes the end state back and takes the next index.
+ * The loop body is ONE force evaluation: a per-slot state machine decides
+ * where that evaluation is (the step's start, node n of predictor-corrector
+ * iteration k) and what to do with the result, so the expensive part (the
+ * ephemeris + force model, ~2k FP64 instructions) runs converged across the
+ * warp while the cheap bookkeeping diverges.
+ *
+ * IAS15 (Rein & Spiegel 2015, MNRAS 446, 1424), as ASSIST runs it through
+ * REBOUND with adaptive_mode = 1 (src/assist.c:446):
+ *   - Gauss-Radau nodes h_1..h_7, acceleration a(h) = a0 + sum_k b_k h^(k+1);
+ *   - predictor-corrector iterations until the change of b_6 relative to the
+ *     largest acceleration drops below 1e-16, stops decreasing (after 2
+ *     iterations), or 12 iterations ran;
+ *   - step-size control dt_new = dt (epsilon / (max|b_6| / max|a|))^(1/7),
+ *     rejection when dt_new < dt/4, growth capped at 4x, optional min_dt;
+ *   - the next step's b predicted from this step's by the polynomial shift
+ *     with the step-size ratio (skipped above ratio 20);
+ *   - compensated summation of position, velocity and time.
+ * Variational particles are integrated with the same coefficients and never
+ * enter the error measures.
+ *
+ * Per-component state lives in a slot-major workspace in HBM/L2
+ * ([field][component][slot], coalesced); per-slot scalars live in registers.
+ * A clock64 watchdog bounds the kernel's run time: a slot whose budget is
+ * spent writes its particle back with ASSIST_GB300_TIMEOUT-like status and exits.
+ */
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+
+#include "device_forces.cuh"
+#include "ias15_constants.h"
+#include "internal.h"
+
+#define AG_ST_OK 0
+#define AG_ST_COVERAGE 1
+#define AG_ST_NONFINITE 2
+#define AG_ST_BUDGET 3
+#define AG_ST_TIMEOUT 5
+
+struct IasTables {
+    double h[8];
+    double rrinv[8][8];      /* 1/(h_n - h_j) */
+    double c[7][7];          /* b_k += c[j][k] * dg_j, k < j */
+    double d[7][7];          /* g_j = b_j + sum_{k>j} d[j][k] b_k */
+    double fx[8][9];         /* position predictor ratios: s_k = s_(k-1) * fx[n][k] */
+    double fv[8][8];         /* velocity predictor ratios */
+};
+__constant__ IasTables ag_ias;
+
+static bool g_tables_ready[64];
+
+/* Build the IAS15 tables on the host (same expressions as the oracle's
+ * predictor: h*(k-1)/(k+1) and h*k/(k+1)). */
+static int ag_ias_tables_init(void) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && g_tables_ready[dev]) return 0;
+    IasTables T;
+    const double h[8] = IAS15_H_INIT;
+    const double rr[28] = IAS15_RR_INIT;
+    const double cc[21] = IAS15_C_INIT;
+    const double dd[21] = IAS15_D_INIT;
+    for (int n = 0; n < 8; n++) T.h[n] = h[n];
+    for (int n = 0; n < 8; n++) for (int j = 0; j < 8; j++) T.rrinv[n][j] = 0.0;
+    int q = 0;
+    for (int n = 1; n < 8; n++) for (int j = 0; j < n; j++) T.rrinv[n][j] = 1.0 / rr[q++];
+    for (int j = 0; j < 7; j++) for (int k = 0; k < 7; k++) { T.c[j][k] = 0.0; T.d[j][k] = 0.0; }
+    q = 0;
+    for (int j = 1; j < 7; j++) for (int k = 0; k < j; k++) T.c[j][k] = cc[q++];
+    for (int j = 0; j < 7; j++) T.c[j][j] = 1.0;
+    q = 0;
+    for (int j = 0; j < 6; j++) for (int k = j + 1; k < 7; k++) T.d[j][k] = dd[q++];
+    for (int j = 0; j < 7; j++) T.d[j][j] = 1.0;
+    for (int n = 0; n < 8; n++) {
+        T.fx[n][0] = T.fx[n][1] = 0.0;
+        for (int k = 2; k < 9; k++) T.fx[n][k] = h[n] * (double)(k - 1) / (double)(k + 1);
+        T.fv[n][0] = 0.0;
+        for (int k = 1; k < 8; k++) T.fv[n][k] = h[n] * (double)k / (double)(k + 1);
+    }
+    cudaError_t e = cudaMemcpyToSymbol(ag_ias, &T, sizeof(T));
+    if (e != cudaSuccess) return (int)e;
+    if (dev >= 0 && dev < 64) g_tables_ready[dev] = true;
+    return 0;
+}
+
+/* workspace fields */
+enum { W_X0 = 0, W_V0, W_A0, W_XC, W_VC, W_B, W_G = W_B + 7, W_E = W_G + 7, W_BR = W_E + 7, W_ER = W_BR + 7, W_NF = W_ER + 7 };
+
+size_t ag_batch_ws_doubles(int nslots, int nv) { return (size_t)W_NF * 3 * (1 + nv) * (size_t)nslots; }
+
+template <int C>
+struct Ws {
+    double* w;
+    int ns, slot;
+    __device__ __forceinline__ double& operator()(int f, int comp) const { return w[((size_t)f * C + comp) * ns + slot]; }
+};
+
+/* b, e from the last accepted step's br, er with step ratio q (the shift of
+ * the acceleration polynomial to the new step). */
+template <int C>
+__device__ __forceinline__ void ag_predict_next(const Ws<C>& W, double ratio) {
+    if (ratio > 20.0) {
+        for (int comp = 0; comp < C; comp++)
+            for (int k = 0; k < 7; k++) { W(W_E + k, comp) = 0.0; W(W_B + k, comp) = 0.0; }
+        return;
+    }
+    double q[8];
+    q[1] = ratio;
+    for (int k = 2; k < 8; k++) q[k] = q[k - 1] * ratio;
+    constexpr double binom[8][8] = {
+        {1, 0, 0, 0, 0, 0, 0, 0}, {1, 1, 0, 0, 0, 0, 0, 0}, {1, 2, 1, 0, 0, 0, 0, 0}, {1, 3, 3, 1, 0, 0, 0, 0},
+        {1, 4, 6, 4, 1, 0, 0, 0}, {1, 5, 10, 10, 5, 1, 0, 0}, {1, 6, 15, 20, 15, 6, 1, 0}, {1, 7, 21, 35, 35, 21, 7, 1}};
+#pragma unroll 1
+    for (int comp = 0; comp < C; comp++) {
+        double br[7], er[7];
+#pragma unroll
+        for (int k = 0; k < 7; k++) { br[k] = W(W_BR + k, comp); er[k] = W(W_ER + k, comp); }
+#pragma unroll
+        for (int j = 0; j < 7; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 6; k >= j; k--) s = fma(br[k], binom[k + 1][j + 1], s);
+            const double e = q[j + 1] * s;
+            W(W_E + j, comp) = e;
+            W(W_B + j, comp) = e + (br[j] - er[j]);
+        }
+    }
+}
+
+template <int NV>
+__global__ void __launch_bounds__(128) ag_k_batch(DevEphem E, ForceCfg cf, AgBatchArgs A) {
+    constexpr int C = 3 * (1 + NV);
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= A.nslots) return;
+    const Ws<C> W{A.ws, A.nslots, slot};
+    const long long clk0 = clock64();
+    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0;
+
+    int pid = -1;
+    double t = 0, tc = 0, dt = 0, dtls = 0, tend = 0, hstep = 0, pc_err = 0, pc_last = 0;
+    double prm[3] = {0.0, 0.0, 0.0};
+    bool has_prm = false;
+    int phase = 0, iters = 0, sub = 0, last = 0, pstat = 0;
+    long long steps = 0;
+    bool stop = false;
+
+    while (true) {
+        if (pid < 0) {
+            if (stop) break;
+            const int qpos = atomicAdd(A.queue, 1);
+            if (qpos >= A.n) break;
+            pid = A.order[qpos];
+            const double* s0 = A.state + 6 * (size_t)pid;
+            for (int k = 0; k < 3; k++) {
+                W(W_X0, k) = s0[k]; W(W_V0, k) = s0[3 + k]; W(W_XC, k) = 0.0; W(W_VC, k) = 0.0;
+            }
+            for (int q = 0; q < NV; q++) {
+                const double* vs = A.var_state + ((size_t)pid * NV + q) * 6;
+                for (int k = 0; k < 3; k++) {
+                    W(W_X0, 3 + 3 * q + k) = vs[k]; W(W_V0, 3 + 3 * q + k) = vs[3 + k];
+                    W(W_XC, 3 + 3 * q + k) = 0.0; W(W_VC, 3 + 3 * q + k) = 0.0;
+                }
+            }
+            for (int comp = 0; comp < C; comp++)
+                for (int k = 0; k < 7; k++) {
+                    W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; W(W_BR + k, comp) = 0.0; W(W_ER + k, comp) = 0.0;
+                }
+            has_prm = false;
+            if (A.params) {
+                prm[0] = A.params[3 * (size_t)pid]; prm[1] = A.params[3 * (size_t)pid + 1]; prm[2] = A.params[3 * (size_t)pid + 2];
+                has_prm = true;
+            }
+            t = A.t0[pid]; tend = A.t_end[pid]; tc = 0.0; dtls = 0.0;
+            dt = (tend >= t ? 1.0 : -1.0) * fabs(A.dt0);
+            steps = 0; pstat = AG_ST_OK; phase = 0;
+            if (t == tend) phase = 3;     /* nothing to integrate */
+            if (phase == 0) {
+                const double rem = (tend - t) - tc;
+                if (fabs(dt) >= fabs(rem)) { hstep = rem; last = 1; } else { hstep = dt; last = 0; }
+            }
+        }
+        if (phase != 3 && A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles) {
+            pstat = AG_ST_TIMEOUT;
+            phase = 3;
+            stop = true;
+        }
+        if (phase != 3) {
+            /* ---- evaluation point: the step start (node 0) or node `sub` */
+            const double hn = phase == 0 ? 0.0 : ag_ias.h[sub];
+            const double tn = phase == 0 ? t : t + (tc + hstep * hn);
+            double sx[9], sv[8];
+            if (phase == 1) {
+                sx[0] = hstep * hn;
+                sx[1] = sx[0] * sx[0] * 0.5;
+#pragma unroll
+                for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * ag_ias.fx[sub][k];
+                sv[0] = hstep * hn;
+#pragma unroll
+                for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * ag_ias.fv[sub][k];
+            }
+            double xp[3], vp[3];
+            for (int k = 0; k < 3; k++) {
+                if (phase == 0) { xp[k] = W(W_X0, k); vp[k] = W(W_V0, k); }
+                else {
+                    double px = sx[8] * W(W_B + 6, k);
+#pragma unroll
+                    for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, k), px);
+                    px = fma(sx[1], W(W_A0, k), px);
+                    px = fma(sx[0], W(W_V0, k), px);
+                    xp[k] = W(W_X0, k) + (px + W(W_XC, k));
+                    double pv = sv[7] * W(W_B + 6, k);
+#pragma unroll
+                    for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(W_B + j, k), pv);
+                    pv = fma(sv[0], W(W_A0, k), pv);
+                    vp[k] = W(W_V0, k) + (pv + W(W_VC, k));
+                }
+            }
+            /* ---- ephemeris + force model at (tn, xp, vp) */
+            ThreadBodies B(E, tn);
+            double at[C];
+            int st;
+            if (NV > 0) {
+                double J[3][6], JA[3][3];
+                bool has_ng;
+                st = ag_forces<ThreadBodies, true>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, J, JA, &has_ng);
+#pragma unroll 1
+                for (int q = 0; q < NV; q++) {
+                    double dxq[3], dvq[3];
+                    for (int k = 0; k < 3; k++) {
+                        const int comp = 3 + 3 * q + k;
+                        if (phase == 0) { dxq[k] = W(W_X0, comp); dvq[k] = W(W_V0, comp); }
+                        else {
+                            double px = sx[8] * W(W_B + 6, comp);
+                            for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, comp), px);
+                            px = fma(sx[1], W(W_A0, comp), px);
+                            px = fma(sx[0], W(W_V0, comp), px);
+                            dxq[k] = W(W_X0, comp) + (px + W(W_XC, comp));
+                            double pv = sv[7] * W(W_B + 6, comp);
+                            for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(W_B + j, comp), pv);
+                            pv = fma(sv[0], W(W_A0, comp), pv);
+                            dvq[k] = W(W_V0, comp) + (pv + W(W_VC, comp));
+                        }
+                    }
+                    for (int a = 0; a < 3; a++) {
+                        double s = J[a][0] * dxq[0];
+                        s = fma(J[a][1], dxq[1], s); s = fma(J[a][2], dxq[2], s);
+                        s = fma(J[a][3], dvq[0], s); s = fma(J[a][4], dvq[1], s); s = fma(J[a][5], dvq[2], s);
+                        at[3 + 3 * q + a] = s;
+                    }
+                }
+            } else {
+                st = ag_forces<ThreadBodies, false>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, nullptr, nullptr, nullptr);
+            }
+            n_ev++;
+            if (st != AG_OK) {
+                pstat = AG_ST_COVERAGE;
+                phase = 3;
+            } else if (phase == 0) {
+                /* ---- step start: a0 and g from the predicted b */
+                for (int comp = 0; comp < C; comp++) {
+                    W(W_A0, comp) = at[comp];
+                    double b[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+#pragma unroll
+                    for (int j = 0; j < 7; j++) {
+                        double s = b[j];
+#pragma unroll
+                        for (int k = j + 1; k < 7; k++) s = fma(b[k], ag_ias.d[j][k], s);
+                        W(W_G + j, comp) = s;
+                    }
+                }
+                phase = 1; iters = 1; sub = 1; pc_last = 1e300; pc_err = 0.0;
+            } else {
+                /* ---- node `sub`: divided difference g_(n-1), then b */
+                const int n = sub;
+                double maxa = 0.0, maxdb = 0.0;
+                for (int comp = 0; comp < C; comp++) {
+                    double gn = (at[comp] - W(W_A0, comp)) * ag_ias.rrinv[n][0];
+                    for (int j = 1; j < n; j++) gn = (gn - W(W_G + j - 1, comp)) * ag_ias.rrinv[n][j];
+                    const double delta = gn - W(W_G + n - 1, comp);
+                    W(W_G + n - 1, comp) = gn;
+                    for (int k = 0; k < n - 1; k++) W(W_B + k, comp) = fma(delta, ag_ias.c[n - 1][k], W(W_B + k, comp));
+                    W(W_B + n - 1, comp) += delta;
+                    if (n == 7 && comp < 3) {
+                        const double aa = fabs(at[comp]);
+                        if (isnormal(aa) && aa > maxa) maxa = aa;
+                        const double db = fabs(delta);
+                        if (isnormal(db) && db > maxdb) maxdb = db;
+                    }
+                }
+                if (n < 7) {
+                    sub = n + 1;
+                } else {
+                    pc_err = maxdb / maxa;
+                    const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+                    if (!conv) {
+                        pc_last = pc_err; iters++; sub = 1;
+                    } else {
+                        n_it += (unsigned long long)iters;
+                        /* ---- step-size control */
+                        double dt_new = hstep;
+                        bool reject = false;
+                        if (A.epsilon > 0.0) {
+                            double ma = 0.0, mb = 0.0;
+                            for (int k = 0; k < 3; k++) {
+                                const double aa = fabs(at[k]);
+                                if (isnormal(aa) && aa > ma) ma = aa;
+                                const double bb = fabs(W(W_B + 6, k));
+                                if (isnormal(bb) && bb > mb) mb = bb;
+                            }
+                            const double err = mb / ma;
+                            const double safety = 0.25;
+                            if (isnormal(err)) dt_new = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
+                            else dt_new = hstep / safety;
+                            if (fabs(dt_new) < A.min_dt) dt_new = copysign(A.min_dt, dt_new);
+                            const double ratio = dt_new / hstep;
+                            if (fabs(ratio) < safety) reject = true;
+                            else if (fabs(ratio) > 1.0 / safety) dt_new = hstep / safety;
+                        }
+                        if (reject) {
+                            n_rej++;
+                            if (dtls != 0.0) ag_predict_next<C>(W, dt_new / dtls);
+                            else
+                                for (int comp = 0; comp < C; comp++)
+                                    for (int k = 0; k < 7; k++) { W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; }
+                            dt = dt_new;
+                        } else {
+                            n_acc++;
+                            /* ---- accept: advance x0, v0, t with compensated sums */
+                            const double h2 = hstep * hstep;
+                            for (int comp = 0; comp < C; comp++) {
+                                double b[7];
+#pragma unroll
+                                for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+                                const double a0 = W(W_A0, comp);
+                                double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
+                                ix = fma(ix, h2, W(W_V0, comp) * hstep);
+                                double y = ix + W(W_XC, comp);
+                                double x0 = W(W_X0, comp);
+                                double s = x0 + y;
+                                W(W_XC, comp) = y - (s - x0);
+                                W(W_X0, comp) = s;
+                                double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
+                                iv = iv * hstep;
+                                y = iv + W(W_VC, comp);
+                                const double v0 = W(W_V0, comp);
+                                s = v0 + y;
+                                W(W_VC, comp) = y - (s - v0);
+                                W(W_V0, comp) = s;
+#pragma unroll
+                                for (int k = 0; k < 7; k++) { W(W_ER + k, comp) = W(W_E + k, comp); W(W_BR + k, comp) = b[k]; }
+                            }
+                            {
+                                const double y = hstep + tc;
+                                const double s = t + y;
+                                tc = y - (s - t);
+                                t = s;
+                            }
+                            dtls = hstep;
+                            ag_predict_next<C>(W, dt_new / hstep);
+                            dt = dt_new;
+                            steps++;
+                            if (last) { t = tend; tc = 0.0; phase = 3; }
+                            else if (A.max_steps > 0 && steps >= A.max_steps) { pstat = AG_ST_BUDGET; phase = 3; }
+                        }
+                        if (phase != 3) {
+                            phase = 0;
+                            const double rem = (tend - t) - tc;
+                            if (fabs(dt) >= fabs(rem)) { hstep = rem; last = 1; } else { hstep = dt; last = 0; }
+                        }
+                    }
+                }
+            }
+        }
+        if (phase == 3) {
+            /* ---- particle finished: write back and free the slot */
+            double* s0 = A.state + 6 * (size_t)pid;
+            bool finite = true;
+            for (int k = 0; k < 3; k++) {
+                s0[k] = W(W_X0, k) + W(W_XC, k);
+                s0[3 + k] = W(W_V0, k) + W(W_VC, k);
+                finite = finite && isfinite(s0[k]) && isfinite(s0[3 + k]);
+            }
+            for (int q = 0; q < NV; q++) {
+                double* vs = A.var_state + ((size_t)pid * NV + q) * 6;
+                for (int k = 0; k < 3; k++) {
+                    vs[k] = W(W_X0, 3 + 3 * q + k) + W(W_XC, 3 + 3 * q + k);
+                    vs[3 + k] = W(W_V0, 3 + 3 * q + k) + W(W_VC, 3 + 3 * q + k);
+                }
+            }
+            if (pstat == AG_ST_OK && !finite) pstat = AG_ST_NONFINITE;
+            if (A.status) A.status[pid] = pstat;
+            pid = -1;
+        }
+    }
+    atomicAdd(&A.counters[0], n_acc);
+    atomicAdd(&A.counters[1], n_rej);
+    atomicAdd(&A.counters[2], n_ev);
+    atomicAdd(&A.counters[3], n_it);
+}
+
+int ag_batch_max_slots(int nv, int tpb) {
+    int dev = 0, sms = 0, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (nv == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_batch<6>, tpb, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_batch<0>, tpb, 0);
+    if (bps < 1) bps = 1;
+    return sms * bps * tpb;
+}
+
+int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int tpb, cudaStream_t s) {
+    int e = ag_ias_tables_init();
+    if (e) return e;
+    if (tpb > 128) tpb = 128;
+    const int blocks = (a.nslots + tpb - 1) / tpb;
+    if (nv == 6) ag_k_batch<6><<<blocks, tpb, 0, s>>>(E, c, a);
+    else ag_k_batch<0><<<blocks, tpb, 0, s>>>(E, c, a);
+    return (int)cudaGetLastError();
+}
+
+/* FP64 FMA throughput of this device (GFLOP/s), measured with independent FMA
+ * chains; the roofline denominator of the FP64-bound kernels. */
+__global__ void ag_k_dfma_probe(double* out, int iters, double a, double b) {
+    double acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = (double)(threadIdx.x + c) * 1e-3;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[c] = fma(acc[c], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) s += acc[c];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+double ag_fp64_probe_gflops(void) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 256, blocks = sms * 8, iters = 4096;
+    double* d = nullptr;
+    if (cudaMalloc(&d, sizeof(double) * threads * blocks) != cudaSuccess) return 0.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    ag_k_dfma_probe<<<blocks, threads>>>(d, 64, 1.0000001, 1e-9);
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+        cudaEventRecord(e0);
+        ag_k_dfma_probe<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    cudaFree(d);
+    return 2.0 * 8 * (double)iters * threads * blocks / (best * 1e-3) / 1e9;
+}

@@ -1,0 +1,532 @@
+/*
+ * kernels_shared.cu -- K3: IAS15 for ONE simulation whose particles share the
+ * step (REBOUND's reb_simulation_integrate with ASSIST attached: the drop-in
+ * path of the CPU reference, src/assist.c:440-446 selects IAS15 with
+ * adaptive_mode = 1).
+ *
+ * All per-particle state stays on the device between steps.  A step is
+ * a start evaluation (node 0) and predictor-corrector iterations of 7 node
+ * evaluations; each node is predict -> force table kernel -> update.  The
+ * update of node 7 also reduces max|delta b6|, max|a| and max|b6| over the
+ * real particles (the global error measures of adaptive_mode = 1) into three
+ * words the host reads back once per iteration to decide convergence,
+ * acceptance and the next step size, with the same rules as the batched
+ * kernel (kernels_ias15.cu).
+ */
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "device_forces.cuh"
+#include "ias15_constants.h"
+#include "internal.h"
+#include "shared_sim.h"
+
+__constant__ double sh_h[8];
+__constant__ double sh_rrinv[8][8];
+__constant__ double sh_c[7][7];
+__constant__ double sh_d[7][7];
+__constant__ double sh_fx[8][9];
+__constant__ double sh_fv[8][8];
+static bool sh_ready[64];
+
+static int sh_tables_init(void) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && sh_ready[dev]) return 0;
+    const double h[8] = IAS15_H_INIT;
+    const double rr[28] = IAS15_RR_INIT;
+    const double cc[21] = IAS15_C_INIT;
+    const double dd[21] = IAS15_D_INIT;
+    double rrinv[8][8] = {{0}}, c[7][7] = {{0}}, d[7][7] = {{0}}, fx[8][9] = {{0}}, fv[8][8] = {{0}};
+    int q = 0;
+    for (int n = 1; n < 8; n++) for (int j = 0; j < n; j++) rrinv[n][j] = 1.0 / rr[q++];
+    q = 0;
+    for (int j = 1; j < 7; j++) for (int k = 0; k < j; k++) c[j][k] = cc[q++];
+    q = 0;
+    for (int j = 0; j < 6; j++) for (int k = j + 1; k < 7; k++) d[j][k] = dd[q++];
+    for (int j = 0; j < 7; j++) { c[j][j] = 1.0; d[j][j] = 1.0; }
+    for (int n = 0; n < 8; n++) {
+        for (int k = 2; k < 9; k++) fx[n][k] = h[n] * (double)(k - 1) / (double)(k + 1);
+        for (int k = 1; k < 8; k++) fv[n][k] = h[n] * (double)k / (double)(k + 1);
+    }
+    if (cudaMemcpyToSymbol(sh_h, h, sizeof(h)) != cudaSuccess) return 1;
+    cudaMemcpyToSymbol(sh_rrinv, rrinv, sizeof(rrinv));
+    cudaMemcpyToSymbol(sh_c, c, sizeof(c));
+    cudaMemcpyToSymbol(sh_d, d, sizeof(d));
+    cudaMemcpyToSymbol(sh_fx, fx, sizeof(fx));
+    cudaMemcpyToSymbol(sh_fv, fv, sizeof(fv));
+    if (dev >= 0 && dev < 64) sh_ready[dev] = true;
+    return (int)cudaGetLastError();
+}
+
+/* field layout: f*(3*stride) + k*stride + i */
+enum { S_X0 = 0, S_V0, S_A0, S_XC, S_VC, S_AT, S_XP, S_VP, S_B, S_G = S_B + 7, S_E = S_G + 7, S_BR = S_E + 7, S_ER = S_BR + 7,
+       S_PX = S_ER + 7, S_PV, S_PA, S_NF };
+
+struct ShView {
+    double* w;
+    int stride;
+    __device__ __forceinline__ double& operator()(int f, int k, int i) const { return w[((size_t)f * 3 + k) * stride + i]; }
+};
+
+__global__ void sh_k_predict(ShView W, int n, int node, double hstep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (node == 0) {
+        for (int k = 0; k < 3; k++) { W(S_XP, k, i) = W(S_X0, k, i); W(S_VP, k, i) = W(S_V0, k, i); }
+        return;
+    }
+    const double hn = sh_h[node];
+    double sx[9], sv[8];
+    sx[0] = hstep * hn;
+    sx[1] = sx[0] * sx[0] * 0.5;
+#pragma unroll
+    for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * sh_fx[node][k];
+    sv[0] = hstep * hn;
+#pragma unroll
+    for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * sh_fv[node][k];
+    for (int k = 0; k < 3; k++) {
+        double px = sx[8] * W(S_B + 6, k, i);
+#pragma unroll
+        for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(S_B + j, k, i), px);
+        px = fma(sx[1], W(S_A0, k, i), px);
+        px = fma(sx[0], W(S_V0, k, i), px);
+        W(S_XP, k, i) = W(S_X0, k, i) + (px + W(S_XC, k, i));
+        double pv = sv[7] * W(S_B + 6, k, i);
+#pragma unroll
+        for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(S_B + j, k, i), pv);
+        pv = fma(sv[0], W(S_A0, k, i), pv);
+        W(S_VP, k, i) = W(S_V0, k, i) + (pv + W(S_VC, k, i));
+    }
+}
+
+__global__ void sh_k_start(ShView W, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int k = 0; k < 3; k++) {
+        W(S_A0, k, i) = W(S_AT, k, i);
+        double b[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
+#pragma unroll
+        for (int j = 0; j < 7; j++) {
+            double s = b[j];
+#pragma unroll
+            for (int q = j + 1; q < 7; q++) s = fma(b[q], sh_d[j][q], s);
+            W(S_G + j, k, i) = s;
+        }
+    }
+}
+
+/* Reductions into red[0..2] (bit patterns of non-negative doubles compare
+ * like unsigned integers): max|delta b6|, max|a|, max|b6| over real particles. */
+__global__ void sh_k_update(ShView W, int n, int n_real, int node, unsigned long long* red) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double mdb = 0.0, ma = 0.0, mb = 0.0;
+    if (i < n) {
+        for (int k = 0; k < 3; k++) {
+            const double at = W(S_AT, k, i);
+            double gn = (at - W(S_A0, k, i)) * sh_rrinv[node][0];
+            for (int j = 1; j < node; j++) gn = (gn - W(S_G + j - 1, k, i)) * sh_rrinv[node][j];
+            const double delta = gn - W(S_G + node - 1, k, i);
+            W(S_G + node - 1, k, i) = gn;
+            for (int q = 0; q < node - 1; q++) W(S_B + q, k, i) = fma(delta, sh_c[node - 1][q], W(S_B + q, k, i));
+            W(S_B + node - 1, k, i) += delta;
+            if (node == 7 && i < n_real) {
+                const double aa = fabs(at), db = fabs(delta), bb = fabs(W(S_B + 6, k, i));
+                if (isnormal(aa) && aa > ma) ma = aa;
+                if (isnormal(db) && db > mdb) mdb = db;
+                if (isnormal(bb) && bb > mb) mb = bb;
+            }
+        }
+    }
+    if (node != 7) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        mdb = fmax(mdb, __shfl_xor_sync(0xffffffffu, mdb, o));
+        ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&red[0], (unsigned long long)__double_as_longlong(mdb));
+        atomicMax(&red[1], (unsigned long long)__double_as_longlong(ma));
+        atomicMax(&red[2], (unsigned long long)__double_as_longlong(mb));
+    }
+}
+
+__device__ __forceinline__ void sh_predict_next(const ShView& W, int i, double ratio) {
+    if (ratio > 20.0) {
+        for (int k = 0; k < 3; k++)
+            for (int q = 0; q < 7; q++) { W(S_E + q, k, i) = 0.0; W(S_B + q, k, i) = 0.0; }
+        return;
+    }
+    double qp[8];
+    qp[1] = ratio;
+    for (int q = 2; q < 8; q++) qp[q] = qp[q - 1] * ratio;
+    constexpr double binom[8][8] = {
+        {1, 0, 0, 0, 0, 0, 0, 0}, {1, 1, 0, 0, 0, 0, 0, 0}, {1, 2, 1, 0, 0, 0, 0, 0}, {1, 3, 3, 1, 0, 0, 0, 0},
+        {1, 4, 6, 4, 1, 0, 0, 0}, {1, 5, 10, 10, 5, 1, 0, 0}, {1, 6, 15, 20, 15, 6, 1, 0}, {1, 7, 21, 35, 35, 21, 7, 1}};
+    for (int k = 0; k < 3; k++) {
+        double br[7], er[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) { br[q] = W(S_BR + q, k, i); er[q] = W(S_ER + q, k, i); }
+#pragma unroll
+        for (int j = 0; j < 7; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int q = 6; q >= j; q--) s = fma(br[q], binom[q + 1][j + 1], s);
+            const double e = qp[j + 1] * s;
+            W(S_E + j, k, i) = e;
+            W(S_B + j, k, i) = e + (br[j] - er[j]);
+        }
+    }
+}
+
+__global__ void sh_k_accept(ShView W, int n, double hstep, double ratio) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double h2 = hstep * hstep;
+    for (int k = 0; k < 3; k++) {
+        double b[7];
+#pragma unroll
+        for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
+        const double a0 = W(S_A0, k, i);
+        /* keep the start-of-step state for dense output */
+        W(S_PX, k, i) = W(S_X0, k, i) + W(S_XC, k, i);
+        W(S_PV, k, i) = W(S_V0, k, i) + W(S_VC, k, i);
+        W(S_PA, k, i) = a0;
+        double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
+        ix = fma(ix, h2, W(S_V0, k, i) * hstep);
+        double y = ix + W(S_XC, k, i);
+        const double x0 = W(S_X0, k, i);
+        double s = x0 + y;
+        W(S_XC, k, i) = y - (s - x0);
+        W(S_X0, k, i) = s;
+        double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
+        iv = iv * hstep;
+        y = iv + W(S_VC, k, i);
+        const double v0 = W(S_V0, k, i);
+        s = v0 + y;
+        W(S_VC, k, i) = y - (s - v0);
+        W(S_V0, k, i) = s;
+#pragma unroll
+        for (int q = 0; q < 7; q++) { W(S_ER + q, k, i) = W(S_E + q, k, i); W(S_BR + q, k, i) = b[q]; }
+    }
+    sh_predict_next(W, i, ratio);
+}
+
+__global__ void sh_k_reject(ShView W, int n, double ratio, int zero) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (zero) {
+        for (int k = 0; k < 3; k++)
+            for (int q = 0; q < 7; q++) { W(S_B + q, k, i) = 0.0; W(S_E + q, k, i) = 0.0; }
+        return;
+    }
+    sh_predict_next(W, i, ratio);
+}
+
+/* ------------------------------------------------------------------ host side */
+
+struct AgSharedSim {
+    int cap = 0;                  /* particle capacity (stride) */
+    double* d_ws = nullptr;
+    double* d_params = nullptr;
+    size_t params_cap = 0;
+    int* d_vstart = nullptr;
+    int* d_vindex = nullptr;
+    int* d_vcfg = nullptr;
+    size_t vcap = 0;
+    unsigned long long* d_red = nullptr;
+    int* d_status = nullptr;
+    cudaStream_t stream = nullptr;
+    double* h_pin = nullptr;      /* pinned staging, 6*cap doubles */
+    int n = 0, n_real = 0;
+    bool state_on_device = false; /* device x0/v0 match sim->particles */
+    double t = 0, tc = 0, dt_last_success = 0, dir = 0;
+};
+
+AgSharedSim* ag_shared_create(void) { return new AgSharedSim(); }
+void ag_shared_free(AgSharedSim* s) {
+    if (!s) return;
+    if (s->d_ws) cudaFree(s->d_ws);
+    if (s->d_params) cudaFree(s->d_params);
+    if (s->d_vstart) cudaFree(s->d_vstart);
+    if (s->d_vindex) cudaFree(s->d_vindex);
+    if (s->d_vcfg) cudaFree(s->d_vcfg);
+    if (s->d_red) cudaFree(s->d_red);
+    if (s->d_status) cudaFree(s->d_status);
+    if (s->h_pin) cudaFreeHost(s->h_pin);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+static int sh_reserve(AgSharedSim* s, int n) {
+    if (!s->stream && ag_cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream")) return 1;
+    if (!s->d_red) {
+        if (ag_cuda_check(cudaMalloc(&s->d_red, 4 * sizeof(unsigned long long)), "cudaMalloc(red)")) return 1;
+        if (ag_cuda_check(cudaMalloc(&s->d_status, sizeof(int)), "cudaMalloc(status)")) return 1;
+    }
+    if (n <= s->cap) return 0;
+    int cap = n < 64 ? 64 : n;
+    double* ws = nullptr;
+    if (ag_cuda_check(cudaMalloc(&ws, sizeof(double) * (size_t)S_NF * 3 * cap), "cudaMalloc(IAS15 state)")) return 1;
+    cudaMemsetAsync(ws, 0, sizeof(double) * (size_t)S_NF * 3 * cap, s->stream);
+    if (s->d_ws) cudaFree(s->d_ws);
+    s->d_ws = ws;
+    if (s->h_pin) cudaFreeHost(s->h_pin);
+    if (ag_cuda_check(cudaMallocHost(&s->h_pin, sizeof(double) * 9 * (size_t)cap), "cudaMallocHost")) return 1;
+    s->cap = cap;
+    s->state_on_device = false;
+    return 0;
+}
+
+/* Upload variational bookkeeping (per real particle: its variational
+ * particles in var_config order) and the Marsden parameters. */
+static int sh_upload_vars(AgSharedSim* s, struct reb_simulation* r, const double* params, AgForceIO* io) {
+    const int n = r->N, n_real = r->N - r->N_var;
+    std::vector<int> cnt((size_t)n_real + 1, 0), start((size_t)n_real + 1, 0);
+    const int nvc = r->N_var_config;
+    for (int v = 0; v < nvc; v++) {
+        const int tp = r->var_config[v].testparticle;
+        if (tp >= 0 && tp < n_real && r->var_config[v].index >= 0 && r->var_config[v].index < n) cnt[(size_t)tp]++;
+    }
+    for (int j = 0; j < n_real; j++) start[(size_t)j + 1] = start[(size_t)j] + cnt[(size_t)j];
+    std::vector<int> idx((size_t)start[(size_t)n_real] + 1), cfg((size_t)start[(size_t)n_real] + 1), fill(start.begin(), start.end());
+    for (int v = 0; v < nvc; v++) {
+        const int tp = r->var_config[v].testparticle;
+        if (tp >= 0 && tp < n_real && r->var_config[v].index >= 0 && r->var_config[v].index < n) {
+            idx[(size_t)fill[(size_t)tp]] = r->var_config[v].index;
+            cfg[(size_t)fill[(size_t)tp]] = v;
+            fill[(size_t)tp]++;
+        }
+    }
+    const size_t nv = (size_t)start[(size_t)n_real];
+    if (n_real + 1 + nv > s->vcap) {
+        if (s->d_vstart) cudaFree(s->d_vstart);
+        if (s->d_vindex) cudaFree(s->d_vindex);
+        if (s->d_vcfg) cudaFree(s->d_vcfg);
+        s->vcap = (size_t)n_real + 1 + nv + 64;
+        if (ag_cuda_check(cudaMalloc(&s->d_vstart, sizeof(int) * s->vcap), "cudaMalloc(vars)") ||
+            ag_cuda_check(cudaMalloc(&s->d_vindex, sizeof(int) * s->vcap), "cudaMalloc(vars)") ||
+            ag_cuda_check(cudaMalloc(&s->d_vcfg, sizeof(int) * s->vcap), "cudaMalloc(vars)"))
+            return 1;
+    }
+    cudaMemcpyAsync(s->d_vstart, start.data(), sizeof(int) * ((size_t)n_real + 1), cudaMemcpyHostToDevice, s->stream);
+    if (nv) {
+        cudaMemcpyAsync(s->d_vindex, idx.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s->stream);
+        cudaMemcpyAsync(s->d_vcfg, cfg.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s->stream);
+    }
+    io->var_start = nv ? s->d_vstart : nullptr;
+    io->var_index = s->d_vindex;
+    io->var_cfg = s->d_vcfg;
+    io->params = nullptr;
+    if (params) {
+        const size_t np = 3 * (size_t)(n_real + nvc);
+        if (np > s->params_cap) {
+            if (s->d_params) cudaFree(s->d_params);
+            s->params_cap = np + 64;
+            if (ag_cuda_check(cudaMalloc(&s->d_params, sizeof(double) * s->params_cap), "cudaMalloc(params)")) return 1;
+        }
+        cudaMemcpyAsync(s->d_params, params, sizeof(double) * np, cudaMemcpyHostToDevice, s->stream);
+        io->params = s->d_params;
+    }
+    /* the host vectors above must outlive the async copies */
+    return ag_cuda_check(cudaStreamSynchronize(s->stream), "upload variational map");
+}
+
+int ag_shared_forces(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, struct reb_simulation* r,
+                     const double* params, int* status_out) {
+    const int n = r->N, n_real = r->N - r->N_var;
+    if (n <= 0) return 0;
+    if (sh_reserve(s, n)) return 1;
+    AgForceIO io;
+    std::memset(&io, 0, sizeof(io));
+    if (sh_upload_vars(s, r, params, &io)) return 1;
+    ShView W{s->d_ws, s->cap};
+    double* h = s->h_pin;
+    for (int i = 0; i < n; i++) {
+        const reb_particle& p = r->particles[i];
+        h[0 * (size_t)s->cap + i] = p.x; h[1 * (size_t)s->cap + i] = p.y; h[2 * (size_t)s->cap + i] = p.z;
+        h[3 * (size_t)s->cap + i] = p.vx; h[4 * (size_t)s->cap + i] = p.vy; h[5 * (size_t)s->cap + i] = p.vz;
+    }
+    double* xp = &W.w[(size_t)S_XP * 3 * s->cap];
+    double* vp = &W.w[(size_t)S_VP * 3 * s->cap];
+    double* at = &W.w[(size_t)S_AT * 3 * s->cap];
+    cudaMemcpyAsync(xp, h, sizeof(double) * 3 * (size_t)s->cap, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(vp, h + 3 * (size_t)s->cap, sizeof(double) * 3 * (size_t)s->cap, cudaMemcpyHostToDevice, s->stream);
+    cudaMemsetAsync(at, 0, sizeof(double) * 3 * (size_t)s->cap, s->stream);
+    cudaMemsetAsync(s->d_status, 0, sizeof(int), s->stream);
+    io.n_real = n_real; io.stride = s->cap; io.x = xp; io.v = vp; io.a = at; io.status = s->d_status;
+    int e = ag_launch_forces_table(E, c, r->t, io, s->stream);
+    if (e) return ag_cuda_check((cudaError_t)e, "force kernel");
+    cudaMemcpyAsync(h + 6 * (size_t)s->cap, at, sizeof(double) * 3 * (size_t)s->cap, cudaMemcpyDeviceToHost, s->stream);
+    int st = 0;
+    cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (ag_cuda_check(cudaStreamSynchronize(s->stream), "force kernel")) return 1;
+    const double* a = h + 6 * (size_t)s->cap;
+    for (int i = 0; i < n; i++) {
+        r->particles[i].ax += a[0 * (size_t)s->cap + i];
+        r->particles[i].ay += a[1 * (size_t)s->cap + i];
+        r->particles[i].az += a[2 * (size_t)s->cap + i];
+    }
+    s->state_on_device = false;
+    *status_out = st;
+    return 0;
+}
+
+/* Integrate r to tmax with IAS15 on the device.  Returns 0 or 1 (CUDA error);
+ * *status_out receives an ASSIST status of the force model. */
+int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, struct reb_simulation* r,
+                        const double* params, double tmax, ShIntegrateOut* out) {
+    const int n = r->N, n_real = r->N - r->N_var;
+    out->status = 0;
+    if (n <= 0 || r->t == tmax) return 0;
+    if (sh_tables_init()) return ag_cuda_check(cudaErrorInvalidValue, "IAS15 tables");
+    if (sh_reserve(s, n)) return 1;
+    AgForceIO io;
+    std::memset(&io, 0, sizeof(io));
+    if (sh_upload_vars(s, r, params, &io)) return 1;
+    ShView W{s->d_ws, s->cap};
+    const size_t F = 3 * (size_t)s->cap;
+    const int tpb = 128, blocks = (n + tpb - 1) / tpb;
+    cudaStream_t st = s->stream;
+    double dir = tmax >= r->t ? 1.0 : -1.0;
+    /* the host particles are authoritative: upload them every call; keep the
+     * predictor state only when this call continues the previous one */
+    const bool cont = s->state_on_device && s->t == r->t && s->n == n && s->dir == dir;
+    {
+        double* h = s->h_pin;
+        for (int i = 0; i < n; i++) {
+            const reb_particle& p = r->particles[i];
+            h[0 * (size_t)s->cap + i] = p.x; h[1 * (size_t)s->cap + i] = p.y; h[2 * (size_t)s->cap + i] = p.z;
+            h[3 * (size_t)s->cap + i] = p.vx; h[4 * (size_t)s->cap + i] = p.vy; h[5 * (size_t)s->cap + i] = p.vz;
+        }
+        cudaMemcpyAsync(W.w + (size_t)S_X0 * F, h, sizeof(double) * F, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(W.w + (size_t)S_V0 * F, h + F, sizeof(double) * F, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(W.w + (size_t)S_XC * F, 0, sizeof(double) * 2 * F, st);
+        if (!cont) {
+            cudaMemsetAsync(W.w + (size_t)S_B * F, 0, sizeof(double) * 35 * F, st);
+            s->dt_last_success = 0.0;
+        }
+        s->t = r->t;
+        s->tc = 0.0;
+        s->n = n;
+        s->dir = dir;
+    }
+    s->n_real = n_real;
+    io.n_real = n_real; io.stride = s->cap;
+    io.x = W.w + (size_t)S_XP * F; io.v = W.w + (size_t)S_VP * F; io.a = W.w + (size_t)S_AT * F;
+    io.status = s->d_status;
+    const double h_nodes[8] = IAS15_H_INIT;
+    double dt = r->dt;
+    if (dt * dir <= 0) dt = dir * std::fabs(dt != 0 ? dt : 0.001);
+    const double eps = r->ri_ias15.epsilon, min_dt = r->ri_ias15.min_dt;
+    unsigned long long red[3];
+    int hstat = 0;
+    long long steps = 0;
+    while (s->t != tmax) {
+        const double rem = (tmax - s->t) - s->tc;
+        bool last = false;
+        double hstep = dt;
+        if (std::fabs(dt) >= std::fabs(rem)) { hstep = rem; last = true; }
+        /* node 0 */
+        cudaMemsetAsync(s->d_status, 0, sizeof(int), st);
+        sh_k_predict<<<blocks, tpb, 0, st>>>(W, n, 0, hstep);
+        ag_launch_forces_table(E, c, s->t, io, st);
+        sh_k_start<<<blocks, tpb, 0, st>>>(W, n);
+        out->evals++;
+        double pc_last = 1e300, pc_err = 0.0;
+        int iters = 1;
+        while (true) {
+            cudaMemsetAsync(s->d_red, 0, 3 * sizeof(unsigned long long), st);
+            for (int node = 1; node < 8; node++) {
+                sh_k_predict<<<blocks, tpb, 0, st>>>(W, n, node, hstep);
+                ag_launch_forces_table(E, c, s->t + (s->tc + hstep * h_nodes[node]), io, st);
+                sh_k_update<<<blocks, tpb, 0, st>>>(W, n, n_real, node, s->d_red);
+                out->evals++;
+            }
+            cudaMemcpyAsync(red, s->d_red, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&hstat, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (ag_cuda_check(cudaStreamSynchronize(st), "IAS15 iteration")) return 1;
+            if (hstat != 0) { out->status = hstat; break; }
+            double mdb, ma;
+            std::memcpy(&mdb, &red[0], 8);
+            std::memcpy(&ma, &red[1], 8);
+            pc_err = mdb / ma;
+            const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+            if (conv) break;
+            pc_last = pc_err;
+            iters++;
+        }
+        if (out->status) break;
+        out->iterations += iters;
+        double mb, ma;
+        std::memcpy(&ma, &red[1], 8);
+        std::memcpy(&mb, &red[2], 8);
+        double dt_new = hstep;
+        bool reject = false;
+        if (eps > 0.0) {
+            const double err = mb / ma;
+            const double safety = 0.25;
+            if (std::isnormal(err)) dt_new = std::pow(eps / err, 1.0 / 7.0) * hstep;
+            else dt_new = hstep / safety;
+            if (std::fabs(dt_new) < min_dt) dt_new = std::copysign(min_dt, dt_new);
+            const double ratio = dt_new / hstep;
+            if (std::fabs(ratio) < safety) reject = true;
+            else if (std::fabs(ratio) > 1.0 / safety) dt_new = hstep / safety;
+        }
+        if (reject) {
+            out->rejected++;
+            if (s->dt_last_success != 0.0) sh_k_reject<<<blocks, tpb, 0, st>>>(W, n, dt_new / s->dt_last_success, 0);
+            else sh_k_reject<<<blocks, tpb, 0, st>>>(W, n, 0.0, 1);
+            dt = dt_new;
+            continue;
+        }
+        sh_k_accept<<<blocks, tpb, 0, st>>>(W, n, hstep, dt_new / hstep);
+        out->accepted++;
+        {
+            const double y = hstep + s->tc;
+            const double sum = s->t + y;
+            s->tc = y - (sum - s->t);
+            s->t = sum;
+        }
+        s->dt_last_success = hstep;
+        out->dt_last_done = hstep;
+        dt = dt_new;
+        steps++;
+        if (last) { s->t = tmax; s->tc = 0.0; }
+        if (out->max_steps > 0 && steps >= out->max_steps && s->t != tmax) { out->status = -1; break; }
+    }
+    /* copy back: current state and the last step's start state / b for dense output */
+    double* h = s->h_pin;
+    cudaMemcpyAsync(h, W.w + (size_t)S_X0 * F, sizeof(double) * 5 * F, cudaMemcpyDeviceToHost, st);
+    if (ag_cuda_check(cudaStreamSynchronize(st), "copy back")) return 1;
+    const double* X0 = h; const double* V0 = h + F; const double* XC = h + 3 * F; const double* VC = h + 4 * F;
+    for (int i = 0; i < n; i++) {
+        reb_particle& p = r->particles[i];
+        p.x = X0[i] + XC[i]; p.y = X0[s->cap + i] + XC[s->cap + i]; p.z = X0[2 * (size_t)s->cap + i] + XC[2 * (size_t)s->cap + i];
+        p.vx = V0[i] + VC[i]; p.vy = V0[s->cap + i] + VC[s->cap + i]; p.vz = V0[2 * (size_t)s->cap + i] + VC[2 * (size_t)s->cap + i];
+    }
+    if (out->dense) {
+        /* start-of-last-step positions, velocities, accelerations and b */
+        std::vector<double> tmp(3 * F);
+        cudaMemcpy(tmp.data(), W.w + (size_t)S_PX * F, sizeof(double) * 3 * F, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                out->dense_x0[3 * i + k] = tmp[(size_t)k * s->cap + i];
+                out->dense_v0[3 * i + k] = tmp[F + (size_t)k * s->cap + i];
+                out->dense_a0[3 * i + k] = tmp[2 * F + (size_t)k * s->cap + i];
+            }
+        std::vector<double> br(7 * F);
+        cudaMemcpy(br.data(), W.w + (size_t)S_BR * F, sizeof(double) * 7 * F, cudaMemcpyDeviceToHost);
+        for (int q = 0; q < 7; q++)
+            for (int i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) out->dense_b[q][3 * i + k] = br[(size_t)q * F + (size_t)k * s->cap + i];
+    }
+    r->t = s->t;
+    r->dt = dt;
+    s->state_on_device = true;
+    return 0;
+}

@@ -270,6 +270,11 @@ int assist_gb300_forces_device(const struct assist_ephem* ephem, const struct as
 int assist_gb300_ephem_device(const struct assist_ephem* ephem, int n, const double* d_t,
                               double* d_out, int* d_status, void* stream);
 
+/* FP64 fused multiply-add throughput of the current CUDA device in GFLOP/s,
+ * measured with independent FMA chains (the roofline denominator of these
+ * FP64-bound kernels). */
+double assist_gb300_fp64_peak_gflops(void);
+
 /* Number of bodies (11 + asteroids) of a loaded ephemeris. */
 int assist_gb300_n_bodies(const struct assist_ephem* ephem);
 

@@ -630,7 +630,10 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
     a.status = d_status; a.ws = g_batch.d_ws; a.counters = g_batch.d_counters;
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
-    a.watchdog_cycles = (long long)(600.0 * 2.2e9);    /* ~10 minutes at the boost clock */
+    /* per-thread run-time budget: ASSIST_GB300_WATCHDOG_S seconds (default 300) at the boost clock */
+    double wd = 300.0;
+    if (const char* w = getenv("ASSIST_GB300_WATCHDOG_S")) wd = atof(w);
+    a.watchdog_cycles = wd > 0 ? (long long)(wd * 2.1e9) : 0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, s);

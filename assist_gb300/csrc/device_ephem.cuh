@@ -66,6 +66,13 @@ struct DevEphem {
     double J2E, J3E, J4E, J2SUN, Re_eq, Rs_eq, c_squared, over_c_squared;
 };
 
+/* isnormal() for a non-negative argument (the IAS15 error measures take
+ * maxima of |a| and |b|): at least the smallest normal double and finite;
+ * false for 0, subnormals, Inf and NaN. */
+__device__ __forceinline__ bool ag_isnormal_pos(double a) {
+    return a >= 2.2250738585072014e-308 && a <= 1.7976931348623157e308;
+}
+
 /* Planet record selection shared by all eleven planets at one time
  * (src/ascii_ephem.c:294-300).  Returns AG_OK or AG_ERR_COVERAGE. */
 __device__ __forceinline__ int ag_planet_record(const DevEphem& E, double t, const double** rec, double* tf) {

@@ -291,9 +291,9 @@ __global__ void __launch_bounds__(128) ag_k_batch(DevEphem E, ForceCfg cf, AgBat
                     W(W_B + n - 1, comp) += delta;
                     if (n == 7 && comp < 3) {
                         const double aa = fabs(at[comp]);
-                        if (isnormal(aa) && aa > maxa) maxa = aa;
+                        if (ag_isnormal_pos(aa) && aa > maxa) maxa = aa;
                         const double db = fabs(delta);
-                        if (isnormal(db) && db > maxdb) maxdb = db;
+                        if (ag_isnormal_pos(db) && db > maxdb) maxdb = db;
                     }
                 }
                 if (n < 7) {
@@ -312,13 +312,13 @@ __global__ void __launch_bounds__(128) ag_k_batch(DevEphem E, ForceCfg cf, AgBat
                             double ma = 0.0, mb = 0.0;
                             for (int k = 0; k < 3; k++) {
                                 const double aa = fabs(at[k]);
-                                if (isnormal(aa) && aa > ma) ma = aa;
+                                if (ag_isnormal_pos(aa) && aa > ma) ma = aa;
                                 const double bb = fabs(W(W_B + 6, k));
-                                if (isnormal(bb) && bb > mb) mb = bb;
+                                if (ag_isnormal_pos(bb) && bb > mb) mb = bb;
                             }
                             const double err = mb / ma;
                             const double safety = 0.25;
-                            if (isnormal(err)) dt_new = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
+                            if (ag_isnormal_pos(err)) dt_new = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
                             else dt_new = hstep / safety;
                             if (fabs(dt_new) < A.min_dt) dt_new = copysign(A.min_dt, dt_new);
                             const double ratio = dt_new / hstep;
@@ -466,4 +466,12 @@ double ag_fp64_probe_gflops(void) {
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     cudaFree(d);
     return 2.0 * 8 * (double)iters * threads * blocks / (best * 1e-3) / 1e9;
+}
+
+/* Copy of the device IAS15 tables (diagnostics: compared with the generated
+ * header by the tests). out: 306 doubles in IasTables order. */
+extern "C" int ag_debug_ias_tables(double* out) {
+    int e = ag_ias_tables_init();
+    if (e) return e;
+    return (int)cudaMemcpyFromSymbol(out, ag_ias, sizeof(IasTables));
 }

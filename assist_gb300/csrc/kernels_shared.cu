@@ -136,9 +136,9 @@ __global__ void sh_k_update(ShView W, int n, int n_real, int node, unsigned long
             W(S_B + node - 1, k, i) += delta;
             if (node == 7 && i < n_real) {
                 const double aa = fabs(at), db = fabs(delta), bb = fabs(W(S_B + 6, k, i));
-                if (isnormal(aa) && aa > ma) ma = aa;
-                if (isnormal(db) && db > mdb) mdb = db;
-                if (isnormal(bb) && bb > mb) mb = bb;
+                if (ag_isnormal_pos(aa) && aa > ma) ma = aa;
+                if (ag_isnormal_pos(db) && db > mdb) mdb = db;
+                if (ag_isnormal_pos(bb) && bb > mb) mb = bb;
             }
         }
     }
@@ -276,7 +276,8 @@ static int sh_reserve(AgSharedSim* s, int n) {
     if (s->d_ws) cudaFree(s->d_ws);
     s->d_ws = ws;
     if (s->h_pin) cudaFreeHost(s->h_pin);
-    if (ag_cuda_check(cudaMallocHost(&s->h_pin, sizeof(double) * 9 * (size_t)cap), "cudaMallocHost")) return 1;
+    /* staging: 5 fields x 3 components (X0, V0, A0, XC, VC) on copy-back */
+    if (ag_cuda_check(cudaMallocHost(&s->h_pin, sizeof(double) * 15 * (size_t)cap), "cudaMallocHost")) return 1;
     s->cap = cap;
     s->state_on_device = false;
     return 0;
@@ -529,4 +530,16 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     r->dt = dt;
     s->state_on_device = true;
     return 0;
+}
+
+/* Copy of the shared-step IAS15 tables (diagnostics). out: h[8], rrinv[64], c[49], d[49], fx[72], fv[64]. */
+extern "C" int ag_debug_shared_tables(double* out) {
+    int e = sh_tables_init();
+    if (e) return e;
+    cudaMemcpyFromSymbol(out, sh_h, sizeof(double) * 8);
+    cudaMemcpyFromSymbol(out + 8, sh_rrinv, sizeof(double) * 64);
+    cudaMemcpyFromSymbol(out + 72, sh_c, sizeof(double) * 49);
+    cudaMemcpyFromSymbol(out + 121, sh_d, sizeof(double) * 49);
+    cudaMemcpyFromSymbol(out + 170, sh_fx, sizeof(double) * 72);
+    return (int)cudaMemcpyFromSymbol(out + 242, sh_fv, sizeof(double) * 64);
 }

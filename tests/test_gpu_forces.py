@@ -1,0 +1,124 @@
+"""Device force model against the oracle (and the reference's golden
+outputs): per-evaluation accelerations and variational accelerations within
+1e-14 relative (||a_gpu - a_ref|| <= 1e-14 ||a_ref|| per particle)."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-14
+
+
+@pytest.fixture(scope="module")
+def dev():
+    import torch
+    assert torch.cuda.is_available()
+    return torch.device("cuda:0")
+
+
+def _eph(paths):
+    from assist_gb300 import Ephem
+    return Ephem(*paths)
+
+
+def test_forces_against_reference_golden(golden, golden_paths, dev):
+    """Drop-in callback (shared time, arbitrary var_config) vs the reference's
+    own assist_additional_forces outputs."""
+    from assist_gb300 import Extras, Simulation
+    eph = _eph(golden_paths)
+    st = golden["force_state"]; vs = golden["force_var_state"]; tp = golden["force_var_tp"]
+    n, m = st.shape[0], vs.shape[0]
+    for c, ref in zip(golden["force_cases"], golden["force_acc"]):
+        flags, gr, geo, with_p = (int(v) for v in c)
+        sim = Simulation.create()
+        ex = Extras(sim, eph)
+        ex._forces = flags
+        ex.gr_eih_sources = gr
+        ex.geocentric = geo
+        for i in range(n):
+            sim.add(*st[i])
+        for k in range(m):
+            idx = sim.add_variation(int(tp[k]))
+            p = sim.particle(idx)
+            p.x, p.y, p.z, p.vx, p.vy, p.vz = vs[k]
+        if with_p:
+            ex.particle_params = golden["force_params"]
+        sim.t = float(golden["force_t"])
+        sim.update_acceleration()
+        assert sim.status <= 0
+        acc = np.array([[p.ax, p.ay, p.az] for p in sim.particles])
+        e = rel_err(acc, ref)
+        assert e[:n].max() < TOL, (hex(flags), e[:n].max())
+        assert e[n:].max() < TOL, (hex(flags), "var", e[n:].max())
+        ex.detach(sim)
+        sim.free()
+
+
+def test_forces_each_time_vs_oracle(synth_files, dev):
+    """Batched evaluation with per-particle times and 6 variational particles each."""
+    import torch
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    rng = np.random.default_rng(0)
+    n = 300
+    pop = synth.population(system, "mix", n, seed=2, t0=8000.0, nongrav_frac=0.3, close_frac=0.02)
+    tt = pop.t0 + rng.uniform(-150.0, 900.0, n)
+    var = rng.normal(size=(n, 6, 6))
+    for flags, gr, geo in [(0x7F, 1, 0), (0x1FF, 11, 0), (0x7F, 4, 1), (0x01, 1, 0), (0x08, 1, 0), (0x10, 1, 0),
+                           (0x20, 1, 0), (0x40, 2, 0), (0x80, 1, 0), (0x100, 1, 0)]:
+        o = batch.options(forces=flags, gr_eih_sources=gr, geocentric=geo)
+        T = torch.tensor(tt, device=dev); S = torch.tensor(pop.state, device=dev)
+        P = torch.tensor(pop.params, device=dev); V = torch.tensor(var, device=dev)
+        acc, vacc = batch.forces_device(eph, T, S, params=P, var_state=V, opts=o)
+        acc = acc.cpu().numpy(); vacc = vacc.cpu().numpy()
+        for i in range(n):
+            ref = O.forces(tt[i], pop.state[i:i + 1], params=pop.params[i:i + 1], var_state=var[i],
+                           var_tp=np.zeros(6, np.int32), forces=flags, gr_eih_sources=gr, geocentric=geo)
+            assert rel_err(acc[i], ref[0]).max() < TOL, (hex(flags), i, rel_err(acc[i], ref[0]))
+            assert rel_err(vacc[i], ref[1:]).max() < TOL, (hex(flags), i, "var")
+
+
+def test_bodies_vs_oracle(synth_files, dev):
+    import torch
+    from assist_gb300 import batch
+    from tests.oracle_py import Oracle
+    pl, ast, _ = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    ts = np.linspace(7800.0, 9000.0, 61)
+    B = batch.bodies_device(eph, torch.tensor(ts, device=dev)).cpu().numpy()
+    for k, t in enumerate(ts):
+        for i in range(27):
+            st, ref = O.body(i, t)
+            assert st == 0
+            m = np.isfinite(ref)
+            assert np.array_equal(np.isfinite(B[k, i]), m)
+            scale = np.abs(ref[m]).max()
+            assert np.abs(B[k, i, m] - ref[m]).max() <= 4e-16 * max(scale, 1.0), (t, i)
+
+
+def test_get_particle_and_coverage(golden, golden_paths, dev):
+    eph = _eph(golden_paths)
+    p = eph.get_particle("Sun", float(golden["body_times"][3]))
+    ref = golden["bodies"][3, 0]
+    assert abs(p.x - ref[1]) < 1e-16 and p.m == ref[0]
+    p = eph.get_particle(20, float(golden["body_times"][5]))
+    assert abs(p.y - golden["bodies"][5, 20, 2]) < 1e-15
+    with pytest.raises(RuntimeError, match="outside the coverage"):
+        eph.get_particle(0, 9999.0)
+    tb, te = eph.time_bounds()
+    assert (tb, te) == (pytest.approx(7968.0), pytest.approx(8256.0))
+
+
+def test_drop_in_coverage_error_sets_status(golden_paths, dev):
+    from assist_gb300 import Extras, Simulation
+    eph = _eph(golden_paths)
+    sim = Simulation.create()
+    ex = Extras(sim, eph)
+    sim.add(2.5, 0.1, 0.0, 0.0, 0.01, 0.0)
+    sim.t = 20000.0
+    sim.update_acceleration()
+    assert sim.status == 1 and b"coverage" in sim.error_message
+    ex.detach(sim); sim.free()

@@ -1,0 +1,146 @@
+"""Device IAS15 (batched persistent kernel and shared-step drop-in) against
+the oracle's IAS15 on the oracle's forces: end states within 1e-9 AU (the
+bar), round trips, variational equations vs finite differences, and the
+error of both paths against the double-double oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+AU_M = 149597870700.0
+
+
+def _eph(paths):
+    from assist_gb300 import Ephem
+    return Ephem(*paths)
+
+
+def test_batch_vs_oracle_mixture(synth_files):
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "mix", 1024, seed=3, t0=8000.0, log_len=(30.0, 900.0), nongrav_frac=0.1,
+                           close_frac=0.01)
+    out, _, status, stats = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params)
+    ref, _, rstat, rstats = O.integrate_batch(pop.t0, pop.t_end, pop.state, params=pop.params, return_all=True)
+    assert (status == 0).all() and (rstat == 0).all()
+    dx = np.abs(out[:, :3] - ref[:, :3]).max(axis=1)
+    assert dx.max() < 1e-9, dx.max()
+    assert np.median(dx) < 1e-12
+    # same algorithm: step counts agree to within a few rejections
+    assert abs(stats["steps_accepted"] - rstats["accepted"]) <= 0.01 * rstats["accepted"]
+
+
+def test_batch_variational_vs_oracle(synth_files):
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "neo", 64, seed=5, t0=8000.0, log_len=(30.0, 400.0))
+    var = np.tile(np.eye(6)[None], (64, 1, 1))
+    out, vout, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, var_state=var)
+    ref, vref, rstat, _ = O.integrate_batch(pop.t0, pop.t_end, pop.state, var_state=var, return_all=True)
+    assert (status == 0).all()
+    assert np.abs(out[:, :3] - ref[:, :3]).max() < 1e-9
+    rel = np.abs(vout - vref).max(axis=(1, 2)) / np.abs(vref).max(axis=(1, 2))
+    assert rel.max() < 1e-7
+
+
+def test_batch_variational_vs_finite_difference(synth_files):
+    """Mirror of the reference's unit_tests/variational_*: 10 m offset vs the
+    variational particle, relative difference < 1e-5 after 1 and 100 days."""
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    p0 = synth.population(system, "mba", 1, seed=6, t0=8000.0).state[0]
+    dx = 10.0 / AU_M
+    p1 = p0.copy(); p1[0] += dx
+    var = np.zeros((2, 6, 6)); var[:, 0, 0] = 1.0
+    for t1 in (8001.0, 8100.0):
+        out, vout, status, _ = batch.integrate_batch(eph, [8000.0, 8000.0], [t1, t1], np.stack([p0, p1]), var_state=var)
+        d1 = out[1, 0] - out[0, 0]
+        d2 = vout[0, 0, 0] * dx
+        assert abs((d1 - d2) / d1) < 1e-5
+
+
+def test_batch_roundtrip(synth_files):
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mix", 256, seed=7, t0=8000.0, length=300.0)
+    fwd, _, s1, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state)
+    back, _, s2, _ = batch.integrate_batch(eph, pop.t_end, pop.t0, fwd)
+    assert (s1 == 0).all() and (s2 == 0).all()
+    assert np.abs(back[:, :3] - pop.state[:, :3]).max() * AU_M < 1.0      # < 1 m over 600 days
+
+
+def test_batch_error_vs_double_double(synth_files):
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "mix", 8, seed=8, t0=8000.0, length=200.0)
+    out, _, _, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state)
+    for i in range(8):
+        dd, _, _ = O.integrate(pop.t0[i], pop.t_end[i], pop.state[i:i + 1], dd=True)
+        assert np.abs(out[i, :3] - dd[0, :3]).max() < 1e-11
+
+
+def test_batch_coverage_status(synth_files):
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mba", 4, seed=9, t0=8000.0)
+    t_end = np.array([8100.0, 20000.0, 8050.0, 8000.0])
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, t_end, pop.state)
+    assert list(status) == [0, 1, 0, 0]
+    assert np.array_equal(out[3], pop.state[3])
+
+
+def test_shared_step_drop_in_vs_oracle(synth_files):
+    from assist_gb300 import Extras, Simulation, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "neo", 48, seed=10, t0=8000.0)
+    sim = Simulation.create(); ex = Extras(sim, eph)
+    for i in range(48):
+        sim.add(*pop.state[i])
+    var_tp = []
+    for i in range(0, 48, 8):
+        for k in range(6):
+            idx = sim.add_variation(i)
+            p = sim.particle(idx)
+            setattr(p, ["x", "y", "z", "vx", "vy", "vz"][k], 1.0)
+            var_tp.append(i)
+    sim.t = 8000.0
+    sim.integrate(8200.0)
+    assert sim.status == 0 and sim.t == 8200.0
+    g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+    var0 = np.zeros((len(var_tp), 6))
+    for q in range(len(var_tp)):
+        var0[q, q % 6] = 1.0
+    r, rv, info = O.integrate(8000.0, 8200.0, pop.state, var_state=var0, var_tp=np.array(var_tp, np.int32))
+    assert np.abs(g[:48, :3] - r[:, :3]).max() < 1e-9
+    rel = np.abs(g[48:] - rv).max() / np.abs(rv).max()
+    assert rel < 1e-7
+    assert sim.steps_done == info["accepted"]
+    ex.detach(sim); sim.free()
+
+
+def test_shared_step_roundtrip(synth_files):
+    """Mirror of the reference's unit_tests/roundtrip_adaptive_*: forward and back."""
+    from assist_gb300 import Extras, Simulation, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mba", 3, seed=11, t0=8000.0)
+    sim = Simulation.create(); ex = Extras(sim, eph)
+    for i in range(3):
+        sim.add(*pop.state[i])
+    sim.t = 8000.0
+    sim.integrate(8500.0)
+    sim.dt = -sim.dt
+    sim.integrate(8000.0)
+    g = np.array([[p.x, p.y, p.z] for p in sim.particles])
+    assert np.abs(g - pop.state[:, :3]).max() * AU_M < 1e-1
+    ex.detach(sim); sim.free()

@@ -44,6 +44,7 @@ const int assist_error_messages_N = ASSIST_ERROR_N;
 
 int ag_ephem_device(const struct assist_ephem* e, DevEphem* out);
 int ag_ephem_n_bodies(const struct assist_ephem* e);
+double ag_sun_gm(const struct assist_ephem* e);
 
 /* ---------------------------------------------------------------- errors */
 static thread_local std::string g_last_error;
@@ -533,6 +534,7 @@ extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
     o->max_steps = 1000000;
     o->warm_start = 0;
     o->threads_per_block = 0;
+    o->group_steps = 1;
 }
 
 extern "C" int assist_gb300_n_bodies(const struct assist_ephem* e) { return ag_ephem_n_bodies(e); }
@@ -564,6 +566,8 @@ extern "C" int assist_gb300_forces_device(const struct assist_ephem* e, const st
 }
 
 struct BatchScratch {
+    int* d_grp = nullptr;           /* grp_start then grp_size */
+    int grp_cap = 0;
     int* d_order = nullptr;
     int* d_queue = nullptr;
     unsigned long long* d_counters = nullptr;
@@ -587,24 +591,112 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     const ForceCfg c = make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
     cudaStream_t s = (cudaStream_t)stream;
     std::lock_guard<std::mutex> lk(g_batch_mu);
-    const int tpb = o->threads_per_block > 0 ? o->threads_per_block : 128;
-    int nslots = ag_batch_max_slots(n_var, tpb);
-    if (nslots > n) nslots = n;
-    /* queue order: longest integrations first, so the last particles taken are short */
-    std::vector<double> t0((size_t)n), te((size_t)n);
+    const bool grouped = o->group_steps != 0;
+    /* block size (independent steps): 128 threads, halved (down to one warp)
+     * while the batch would leave SMs idle */
+    int tpb = o->threads_per_block > 0 ? o->threads_per_block : 128;
+    if (o->threads_per_block <= 0) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        while (tpb > 32 && (n + tpb - 1) / tpb < sms) tpb /= 2;
+    }
+    std::vector<double> t0((size_t)n), te((size_t)n), st0;
     if (ag_cuda_check(cudaMemcpyAsync(t0.data(), d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
-        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end") ||
-        ag_cuda_check(cudaStreamSynchronize(s), "read times"))
+        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end"))
         return ASSIST_ERROR_EPHEM_FILE;
-    std::vector<int> order((size_t)n);
+    if (grouped) {
+        st0.resize(6 * (size_t)n);
+        if (ag_cuda_check(cudaMemcpyAsync(st0.data(), d_state, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, s), "read state"))
+            return ASSIST_ERROR_EPHEM_FILE;
+    }
+    if (ag_cuda_check(cudaStreamSynchronize(s), "read inputs")) return ASSIST_ERROR_EPHEM_FILE;
+    std::vector<int> order((size_t)n), gstart, gsize;
     for (int i = 0; i < n; i++) order[(size_t)i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
-    });
+    if (!grouped) {
+        /* queue order: longest integrations first, so the last particles taken are short */
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
+        });
+    } else {
+        /* groups share t0 and direction; within them particles of similar
+         * orbital timescale (perihelion distance q^1.5, quarter-octave bins)
+         * and similar length sit together; groups are queued longest first */
+        const double gm = e->ascii_planets ? ag_sun_gm(e) : 2.9591220828411951e-04;
+        std::vector<int> bucket((size_t)n);
+        for (int i = 0; i < n; i++) {
+            const double* p = &st0[6 * (size_t)i];
+            const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+            const double v2 = p[3] * p[3] + p[4] * p[4] + p[5] * p[5];
+            const double rv = p[0] * p[3] + p[1] * p[4] + p[2] * p[5];
+            double ev[3];
+            for (int k = 0; k < 3; k++) ev[k] = ((v2 - gm / r) * p[k] - rv * p[3 + k]) / gm;
+            const double ecc = std::sqrt(ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+            const double inv_a = 2.0 / r - v2 / gm;
+            double q = (std::fabs(inv_a) > 1e-12) ? (1.0 - ecc) / inv_a : r;
+            if (!(q > 1e-4)) q = 1e-4;
+            bucket[(size_t)i] = (int)std::floor(4.0 * std::log2(std::pow(q, 1.5)));
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            if (t0[(size_t)a] != t0[(size_t)b]) return t0[(size_t)a] < t0[(size_t)b];
+            const bool fa = te[(size_t)a] >= t0[(size_t)a], fb = te[(size_t)b] >= t0[(size_t)b];
+            if (fa != fb) return fa;
+            if (bucket[(size_t)a] != bucket[(size_t)b]) return bucket[(size_t)a] < bucket[(size_t)b];
+            return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
+        });
+        int i = 0;
+        while (i < n) {
+            const int a = order[(size_t)i];
+            int j = i + 1;
+            while (j < n && j - i < 32) {
+                const int b = order[(size_t)j];
+                if (t0[(size_t)b] != t0[(size_t)a] || (te[(size_t)b] >= t0[(size_t)b]) != (te[(size_t)a] >= t0[(size_t)a]) ||
+                    bucket[(size_t)b] != bucket[(size_t)a])
+                    break;
+                j++;
+            }
+            gstart.push_back(i);
+            gsize.push_back(j - i);
+            i = j;
+        }
+        /* longest group first */
+        std::vector<int> gi(gstart.size());
+        for (size_t k = 0; k < gi.size(); k++) gi[k] = (int)k;
+        auto glen = [&](int g) {
+            double m = 0;
+            for (int k = 0; k < gsize[(size_t)g]; k++) {
+                const int p = order[(size_t)(gstart[(size_t)g] + k)];
+                m = std::max(m, std::fabs(te[(size_t)p] - t0[(size_t)p]));
+            }
+            return m;
+        };
+        std::vector<double> gl(gi.size());
+        for (size_t k = 0; k < gi.size(); k++) gl[k] = glen((int)k);
+        std::stable_sort(gi.begin(), gi.end(), [&](int a, int b) { return gl[(size_t)a] > gl[(size_t)b]; });
+        std::vector<int> s2(gi.size()), z2(gi.size());
+        for (size_t k = 0; k < gi.size(); k++) { s2[k] = gstart[(size_t)gi[k]]; z2[k] = gsize[(size_t)gi[k]]; }
+        gstart.swap(s2);
+        gsize.swap(z2);
+    }
+    int nslots;
+    if (grouped) {
+        nslots = ag_group_max_slots(n_var);
+        const int need = 32 * (int)gstart.size();
+        if (nslots > need) nslots = ((need + 127) / 128) * 128;
+    } else {
+        nslots = ag_batch_max_slots(n_var, tpb);
+        if (nslots > n) nslots = n;
+    }
     if (g_batch.order_cap < n) {
         if (g_batch.d_order) cudaFree(g_batch.d_order);
         if (ag_cuda_check(cudaMalloc(&g_batch.d_order, sizeof(int) * (size_t)n), "cudaMalloc(order)")) return ASSIST_ERROR_EPHEM_FILE;
         g_batch.order_cap = n;
+    }
+    const int ng = (int)gstart.size();
+    if (grouped && g_batch.grp_cap < ng) {
+        if (g_batch.d_grp) cudaFree(g_batch.d_grp);
+        if (ag_cuda_check(cudaMalloc(&g_batch.d_grp, sizeof(int) * 2 * (size_t)ng), "cudaMalloc(groups)")) return ASSIST_ERROR_EPHEM_FILE;
+        g_batch.grp_cap = ng;
     }
     if (!g_batch.d_queue) {
         if (ag_cuda_check(cudaMalloc(&g_batch.d_queue, sizeof(int)), "cudaMalloc") ||
@@ -622,6 +714,10 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
         g_batch.ws_cap = wsn;
     }
     cudaMemcpyAsync(g_batch.d_order, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s);
+    if (grouped) {
+        cudaMemcpyAsync(g_batch.d_grp, gstart.data(), sizeof(int) * (size_t)ng, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(g_batch.d_grp + ng, gsize.data(), sizeof(int) * (size_t)ng, cudaMemcpyHostToDevice, s);
+    }
     cudaMemsetAsync(g_batch.d_queue, 0, sizeof(int), s);
     cudaMemsetAsync(g_batch.d_counters, 0, 8 * sizeof(unsigned long long), s);
     AgBatchArgs a;
@@ -630,6 +726,7 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
     a.status = d_status; a.ws = g_batch.d_ws; a.counters = g_batch.d_counters;
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
+    if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
     /* per-thread run-time budget: ASSIST_GB300_WATCHDOG_S seconds (default 300) at the boost clock */
     double wd = 300.0;
     if (const char* w = getenv("ASSIST_GB300_WATCHDOG_S")) wd = atof(w);
@@ -637,7 +734,7 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int le = ag_launch_batch(D, c, a, n_var, tpb, s);
+    int le = grouped ? ag_launch_group(D, c, a, n_var, s) : ag_launch_batch(D, c, a, n_var, tpb, s);
     cudaEventRecord(e1, s);
     if (le) { cudaEventDestroy(e0); cudaEventDestroy(e1); ag_cuda_check((cudaError_t)le, "batch kernel launch"); return ASSIST_ERROR_EPHEM_FILE; }
     if (stats) {

@@ -33,6 +33,7 @@ enum { AG_C_MER = 0, AG_C_VEN, AG_C_EMB, AG_C_MAR, AG_C_JUP, AG_C_SAT, AG_C_URA,
  * call (src/spk.c:432-445) done once on the host with the same operations. */
 struct AgSpkSeg {
     double init_jd;              /* 2451545 + INIT/86400 */
+    double intlen_days;          /* INTLEN/86400 */
     double inv_intlen_days;      /* 86400/INTLEN */
     long long data_off;          /* 0-based index of the first record's MID in the file */
     int nrec, R, P;
@@ -51,6 +52,8 @@ struct DevEphem {
     int col_off[13], col_ncf[13], col_niv[13];   /* 0-based offsets within a record */
     double gm[AG_NPL];
     double inv_cau;              /* 1/AU[km] */
+    double cau_per_day;          /* AU[km]/86400 (velocity divisor of the exact path) */
+    double f_earth, f_moon;      /* -1/(1+EMRAT), EMRAT/(1+EMRAT) */
     double col_vscale[13];       /* (2*niv/inc/86400) * 86400/AU: d/dtau -> AU/day */
     int pl_inc_pow2;             /* record length is a power of two: divide by multiplying */
     double pl_inv_inc;
@@ -61,9 +64,13 @@ struct DevEphem {
     double ast_beg[AG_MAX_AST], ast_end[AG_MAX_AST], ast_res[AG_MAX_AST], ast_gm[AG_MAX_AST];
     int ast_nseg[AG_MAX_AST], ast_seg0[AG_MAX_AST];
     const struct AgSpkSeg* segs; /* per segment, see AgSpkSeg */
-    const double2* rec_meta;     /* per SPK record: (MID as JD, 86400/RADIUS) */
+    const double4* rec_meta;     /* per SPK record: (MID as JD, RADIUS/86400, 86400/RADIUS, 0) */
     /* constants (ASSIST src/assist.c:296-309) */
     double J2E, J3E, J4E, J2SUN, Re_eq, Rs_eq, c_squared, over_c_squared;
+    /* device copy of this view: kernels read the ephemeris through it (a
+     * by-value kernel parameter indexed with run-time indices would be
+     * copied into every thread's local memory) */
+    const struct DevEphem* self_dev;
 };
 
 /* isnormal() for a non-negative argument (the IAS15 error measures take
@@ -127,36 +134,6 @@ __device__ __forceinline__ void ag_column(const DevEphem& E, const double* rec, 
     }
 }
 
-/* One .440 column: position, velocity and acceleration (U = d2T/dtau2). */
-__device__ __forceinline__ void ag_column_pva(const DevEphem& E, const double* rec, int col, double tf,
-                                              double* u, double* v, double* w) {
-    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
-    const double tt = tf * (double)niv;
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;
-    const double tau = 2.0 * (tt - fl) - 1.0;
-    const double* P = rec + E.col_off[col] + ncf * 3 * b;
-    double T[AG_MAX_NCF], S[AG_MAX_NCF], U[AG_MAX_NCF];
-    T[0] = 1.0; T[1] = tau; S[0] = 0.0; S[1] = 1.0; U[0] = 0.0; U[1] = 0.0; U[2] = 4.0;
-    for (int p = 2; p < ncf; p++) {
-        T[p] = 2.0 * tau * T[p - 1] - T[p - 2];
-        S[p] = 2.0 * tau * S[p - 1] + 2.0 * T[p - 1] - S[p - 2];
-    }
-    for (int p = 3; p < ncf; p++) U[p] = 2.0 * tau * U[p - 1] + 4.0 * S[p - 1] - U[p - 2];
-    const double c = (double)(niv * 2) / E.pl_inc / 86400.0;
-    for (int m = 0; m < 3; m++) {
-        double su = 0.0, sv = 0.0, sw = 0.0;
-        for (int p = 0; p < ncf; p++) {
-            const double cf = P[m * ncf + p];
-            su = fma(T[p], cf, su);
-            sv = fma(S[p], cf, sv);
-            sw = fma(U[p], cf, sw);
-        }
-        u[m] = su; v[m] = sv * c; w[m] = sw * (c * c);
-    }
-}
-
 /* Column of ASSIST body index (Earth and Moon are handled by the caller). */
 __device__ __forceinline__ int ag_col_of(int body) {
     switch (body) {
@@ -173,30 +150,9 @@ __device__ __forceinline__ int ag_col_of(int body) {
 }
 
 /* Full state of planet `body` (0..10): GM, position, velocity, acceleration
- * in AU and days, as assist_ascii_calc returns them. */
-__device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out) {
-    const double* rec;
-    double tf;
-    out[0] = E.gm[body];
-    int st = ag_planet_record(E, t, &rec, &tf);
-    if (st != AG_OK) return st;
-    double u[3], v[3], w[3];
-    if (body == AG_EAR || body == AG_MOO) {
-        double eu[3], ev[3], ew[3], lu[3], lv[3], lw[3];
-        ag_column_pva(E, rec, AG_C_EMB, tf, eu, ev, ew);
-        ag_column_pva(E, rec, AG_C_LUN, tf, lu, lv, lw);
-        const double f = body == AG_EAR ? -1.0 / (1.0 + E.pl_cem) : E.pl_cem / (1.0 + E.pl_cem);
-        for (int k = 0; k < 3; k++) { u[k] = eu[k] + lu[k] * f; v[k] = ev[k] + lv[k] * f; w[k] = ew[k] + lw[k] * f; }
-    } else {
-        ag_column_pva(E, rec, ag_col_of(body), tf, u, v, w);
-    }
-    for (int k = 0; k < 3; k++) {
-        out[1 + k] = u[k] / E.pl_cau;
-        out[4 + k] = v[k] / (E.pl_cau / 86400.);
-        out[7 + k] = w[k] / (E.pl_cau / (86400. * 86400.));
-    }
-    return AG_OK;
-}
+ * in AU and days, with the exact arithmetic of assist_ascii_calc
+ * (defined after the exact column evaluator below). */
+__device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out);
 
 /* Heliocentric asteroid position (AU) from its SPK type-2 segment
  * (src/spk.c:428-474): segment n from the target's epoch step, record b,
@@ -214,10 +170,10 @@ __device__ __forceinline__ int ag_asteroid_pos(const DevEphem& E, int m, double 
     int b = (int)(((E.jd_ref - sg.init_jd) + t) * sg.inv_intlen_days);
     if (b >= sg.nrec) b = sg.nrec - 1;
     if (b < 0) b = 0;
-    const double2 meta = E.rec_meta[sg.meta_off + b];
+    const double4 meta = E.rec_meta[sg.meta_off + b];
     const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2;
     const int P = sg.P;
-    const double z = ((E.jd_ref - meta.x) + t) * meta.y;
+    const double z = ((E.jd_ref - meta.x) + t) * meta.z;
     const double two_z = 2.0 * z;
     double T0 = 1.0, T1 = z;
     double px = fma(z, X[1], X[0]), py = fma(z, X[P + 1], X[P]), pz = fma(z, X[2 * P + 1], X[2 * P]);
@@ -231,6 +187,173 @@ __device__ __forceinline__ int ag_asteroid_pos(const DevEphem& E, int m, double 
     }
     const double s = 1.0 / 149597870.7;
     p[0] = px * s; p[1] = py * s; p[2] = pz * s;
+    return AG_OK;
+}
+
+/* ---------------------------------------------------------------------------
+ * Exact evaluators: ASSIST's arithmetic operation for operation (no FMA
+ * contraction, the same association, true IEEE divisions), so body states
+ * agree with the reference bit for bit.  Used wherever a body is evaluated
+ * once for many particles (per-time tables); close approaches need it:
+ * 1 ulp of the Earth's position (1e-16 AU) is a 1e-12 relative change of the
+ * acceleration of a particle 1e-4 AU from the Earth.
+ * ------------------------------------------------------------------------- */
+
+/* .440 column in km and km/s (src/ascii_ephem.c:27-65). */
+template <bool VEL>
+__device__ __forceinline__ void ag_column_exact(const DevEphem& E, const double* rec, int col, double tf, double* u,
+                                                double* v) {
+    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
+    const double tt = __dmul_rn(tf, (double)niv);
+    const double fl = floor(tt);
+    int b = (int)tt;
+    if (b >= niv) b = niv - 1;
+    const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
+    const double two_t0 = __dmul_rn(2.0, t0);
+    const double* P = rec + E.col_off[col] + ncf * 3 * b;
+    double ux = 0.0, uy = 0.0, uz = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+    double c = 0.0;
+    if (VEL) c = __ddiv_rn(__ddiv_rn((double)(niv * 2), E.pl_inc), 86400.0);
+    double T0 = 1.0, T1 = t0, S0 = 0.0, S1 = 1.0;
+    for (int p = 0; p < ncf; p++) {
+        double Tp, Sp;
+        if (p == 0) { Tp = 1.0; Sp = 0.0; }
+        else if (p == 1) { Tp = t0; Sp = 1.0; }
+        else {
+            Tp = __dsub_rn(__dmul_rn(two_t0, T1), T0);
+            if (VEL) Sp = __dsub_rn(__dadd_rn(__dmul_rn(two_t0, S1), __dmul_rn(2.0, T1)), S0);
+            T0 = T1; T1 = Tp;
+            if (VEL) { S0 = S1; S1 = Sp; }
+        }
+        ux = __dadd_rn(ux, __dmul_rn(Tp, P[p]));
+        uy = __dadd_rn(uy, __dmul_rn(Tp, P[ncf + p]));
+        uz = __dadd_rn(uz, __dmul_rn(Tp, P[2 * ncf + p]));
+        if (VEL) {
+            vx = __dadd_rn(vx, __dmul_rn(__dmul_rn(Sp, P[p]), c));
+            vy = __dadd_rn(vy, __dmul_rn(__dmul_rn(Sp, P[ncf + p]), c));
+            vz = __dadd_rn(vz, __dmul_rn(__dmul_rn(Sp, P[2 * ncf + p]), c));
+        }
+    }
+    u[0] = ux; u[1] = uy; u[2] = uz;
+    if (VEL) { v[0] = vx; v[1] = vy; v[2] = vz; }
+}
+
+/* Planet `body` position (AU) and, if VEL, velocity (AU/day), exactly as
+ * assist_ascii_calc forms them (src/ascii_ephem.c:302-380). */
+template <bool VEL>
+__device__ __forceinline__ void ag_planet_exact(const DevEphem& E, const double* rec, double tf, int body, double* x,
+                                                double* v) {
+    double u[3], w[3];
+    if (body == AG_EAR || body == AG_MOO) {
+        double eu[3], ev[3], lu[3], lv[3];
+        ag_column_exact<VEL>(E, rec, AG_C_EMB, tf, eu, ev);
+        ag_column_exact<VEL>(E, rec, AG_C_LUN, tf, lu, lv);
+        const double f = body == AG_EAR ? E.f_earth : E.f_moon;
+        for (int k = 0; k < 3; k++) {
+            u[k] = __dadd_rn(eu[k], __dmul_rn(lu[k], f));
+            if (VEL) w[k] = __dadd_rn(ev[k], __dmul_rn(lv[k], f));
+        }
+    } else {
+        ag_column_exact<VEL>(E, rec, ag_col_of(body), tf, u, w);
+    }
+    for (int k = 0; k < 3; k++) {
+        x[k] = __ddiv_rn(u[k], E.pl_cau);
+        if (VEL) v[k] = __ddiv_rn(w[k], E.cau_per_day);
+    }
+}
+
+/* .440 column position, velocity and acceleration (U = d2T/dtau2) with the
+ * exact arithmetic of src/ascii_ephem.c:27-65 (km, km/s, km/s^2). */
+__device__ __forceinline__ void ag_column_pva_exact(const DevEphem& E, const double* rec, int col, double tf, double* u,
+                                                    double* v, double* w) {
+    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
+    const double tt = __dmul_rn(tf, (double)niv);
+    const double fl = floor(tt);
+    int b = (int)tt;
+    if (b >= niv) b = niv - 1;
+    const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
+    const double two_t0 = __dmul_rn(2.0, t0);
+    const double c = __ddiv_rn(__ddiv_rn((double)(niv * 2), E.pl_inc), 86400.0);
+    const double* P = rec + E.col_off[col] + ncf * 3 * b;
+    double T[AG_MAX_NCF], S[AG_MAX_NCF], U[AG_MAX_NCF];
+    T[0] = 1.0; T[1] = t0; S[0] = 0.0; S[1] = 1.0; U[0] = 0.0; U[1] = 0.0; U[2] = 4.0;
+    for (int p = 2; p < ncf; p++) {
+        T[p] = __dsub_rn(__dmul_rn(two_t0, T[p - 1]), T[p - 2]);
+        S[p] = __dsub_rn(__dadd_rn(__dmul_rn(two_t0, S[p - 1]), __dmul_rn(2.0, T[p - 1])), S[p - 2]);
+    }
+    for (int p = 3; p < ncf; p++)
+        U[p] = __dsub_rn(__dadd_rn(__dmul_rn(two_t0, U[p - 1]), __dmul_rn(4.0, S[p - 1])), U[p - 2]);
+    for (int m = 0; m < 3; m++) {
+        double su = 0.0, sv = 0.0, sw = 0.0;
+        for (int p = 0; p < ncf; p++) {
+            const double cf = P[m * ncf + p];
+            su = __dadd_rn(su, __dmul_rn(T[p], cf));
+            sv = __dadd_rn(sv, __dmul_rn(__dmul_rn(S[p], cf), c));
+            sw = __dadd_rn(sw, __dmul_rn(__dmul_rn(__dmul_rn(U[p], cf), c), c));
+        }
+        u[m] = su; v[m] = sv; w[m] = sw;
+    }
+}
+
+__device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out) {
+    const double* rec;
+    double tf;
+    out[0] = E.gm[body];
+    int st = ag_planet_record(E, t, &rec, &tf);
+    if (st != AG_OK) return st;
+    double u[3], v[3], w[3];
+    if (body == AG_EAR || body == AG_MOO) {
+        double eu[3], ev[3], ew[3], lu[3], lv[3], lw[3];
+        ag_column_pva_exact(E, rec, AG_C_EMB, tf, eu, ev, ew);
+        ag_column_pva_exact(E, rec, AG_C_LUN, tf, lu, lv, lw);
+        const double f = body == AG_EAR ? E.f_earth : E.f_moon;
+        for (int k = 0; k < 3; k++) {
+            u[k] = __dadd_rn(eu[k], __dmul_rn(lu[k], f));
+            v[k] = __dadd_rn(ev[k], __dmul_rn(lv[k], f));
+            w[k] = __dadd_rn(ew[k], __dmul_rn(lw[k], f));
+        }
+    } else {
+        ag_column_pva_exact(E, rec, ag_col_of(body), tf, u, v, w);
+    }
+    const double acc_div = E.pl_cau / (86400. * 86400.);
+    for (int k = 0; k < 3; k++) {
+        out[1 + k] = __ddiv_rn(u[k], E.pl_cau);
+        out[4 + k] = __ddiv_rn(v[k], E.cau_per_day);
+        out[7 + k] = __ddiv_rn(w[k], acc_div);
+    }
+    return AG_OK;
+}
+
+/* Asteroid heliocentric position (AU), exactly as assist_spk_calc forms it
+ * (src/spk.c:428-474). */
+__device__ __forceinline__ int ag_asteroid_exact(const DevEphem& E, int m, double t, double* p) {
+    const double jd = E.jd_ref + t;
+    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    int n = 0;
+    if (E.ast_nseg[m] > 1) {
+        n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);
+        if (n >= E.ast_nseg[m]) n = E.ast_nseg[m] - 1;
+    }
+    const AgSpkSeg sg = E.segs[E.ast_seg0[m] + n];
+    int b = (int)(__ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, sg.init_jd), t), sg.intlen_days));
+    if (b >= sg.nrec) b = sg.nrec - 1;
+    if (b < 0) b = 0;
+    const double4 meta = E.rec_meta[sg.meta_off + b];
+    const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2;
+    const int P = sg.P;
+    const double z = __ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, meta.x), t), meta.y);
+    const double two_z = __dmul_rn(2.0, z);
+    double px = 0.0, py = 0.0, pz = 0.0, T0 = 1.0, T1 = z;
+    for (int q = 0; q < P; q++) {
+        double Tq;
+        if (q == 0) Tq = 1.0;
+        else if (q == 1) Tq = z;
+        else { Tq = __dsub_rn(__dmul_rn(two_z, T1), T0); T0 = T1; T1 = Tq; }
+        px = __dadd_rn(px, __dmul_rn(X[q], Tq));
+        py = __dadd_rn(py, __dmul_rn(X[P + q], Tq));
+        pz = __dadd_rn(pz, __dmul_rn(X[2 * P + q], Tq));
+    }
+    p[0] = __ddiv_rn(px, 149597870.7); p[1] = __ddiv_rn(py, 149597870.7); p[2] = __ddiv_rn(pz, 149597870.7);
     return AG_OK;
 }
 

@@ -77,37 +77,43 @@ __device__ __forceinline__ void ag_eih_source(const DevEphem& E, const PlanetSta
 }
 
 /* Evaluate the eleven planets (positions; velocities of the Sun and the first
- * n_vel bodies; Earth's acceleration when geocentric) at time t. */
+ * n_vel bodies; Earth's acceleration when geocentric) at time t with the
+ * exact arithmetic of the reference. */
 __device__ __forceinline__ int ag_planets_at(const DevEphem& E, double t, int n_vel, bool earth_acc, PlanetState& P) {
     const double* rec;
     double tf;
     int st = ag_planet_record(E, t, &rec, &tf);
     if (st != AG_OK) return st;
-    const double s = E.inv_cau;
     double u[3], v[3];
 #pragma unroll 1
     for (int b = 0; b < AG_NPL; b++) {
         if (b == AG_EAR || b == AG_MOO) continue;
-        const int col = ag_col_of(b);
         if (b == AG_SUN || b < n_vel) {
-            ag_column<true>(E, rec, col, tf, u, v);
-            P.vx[b] = v[0] * 1.0; P.vy[b] = v[1]; P.vz[b] = v[2];
+            ag_planet_exact<true>(E, rec, tf, b, u, v);
+            P.vx[b] = v[0]; P.vy[b] = v[1]; P.vz[b] = v[2];
         } else {
-            ag_column<false>(E, rec, col, tf, u, v);
+            ag_planet_exact<false>(E, rec, tf, b, u, v);
         }
-        P.x[b] = u[0] * s; P.y[b] = u[1] * s; P.z[b] = u[2] * s;
+        P.x[b] = u[0]; P.y[b] = u[1]; P.z[b] = u[2];
     }
-    /* Earth and Moon from the Earth-Moon barycentre and the geocentric Moon */
+    /* Earth and Moon share the EMB and geocentric-Moon columns */
     const bool vel_em = n_vel > AG_EAR;
     double eu[3], ev[3], lu[3], lv[3];
-    if (vel_em) { ag_column<true>(E, rec, AG_C_EMB, tf, eu, ev); ag_column<true>(E, rec, AG_C_LUN, tf, lu, lv); }
-    else { ag_column<false>(E, rec, AG_C_EMB, tf, eu, ev); ag_column<false>(E, rec, AG_C_LUN, tf, lu, lv); }
-    const double fe = -1.0 / (1.0 + E.pl_cem), fm = E.pl_cem / (1.0 + E.pl_cem);
-    P.x[AG_EAR] = fma(lu[0], fe, eu[0]) * s; P.y[AG_EAR] = fma(lu[1], fe, eu[1]) * s; P.z[AG_EAR] = fma(lu[2], fe, eu[2]) * s;
-    P.x[AG_MOO] = fma(lu[0], fm, eu[0]) * s; P.y[AG_MOO] = fma(lu[1], fm, eu[1]) * s; P.z[AG_MOO] = fma(lu[2], fm, eu[2]) * s;
-    if (vel_em) {
-        P.vx[AG_EAR] = fma(lv[0], fe, ev[0]); P.vy[AG_EAR] = fma(lv[1], fe, ev[1]); P.vz[AG_EAR] = fma(lv[2], fe, ev[2]);
-        P.vx[AG_MOO] = fma(lv[0], fm, ev[0]); P.vy[AG_MOO] = fma(lv[1], fm, ev[1]); P.vz[AG_MOO] = fma(lv[2], fm, ev[2]);
+    if (vel_em) { ag_column_exact<true>(E, rec, AG_C_EMB, tf, eu, ev); ag_column_exact<true>(E, rec, AG_C_LUN, tf, lu, lv); }
+    else { ag_column_exact<false>(E, rec, AG_C_EMB, tf, eu, ev); ag_column_exact<false>(E, rec, AG_C_LUN, tf, lu, lv); }
+    for (int k = 0; k < 3; k++) {
+        const double xe = __ddiv_rn(__dadd_rn(eu[k], __dmul_rn(lu[k], E.f_earth)), E.pl_cau);
+        const double xm = __ddiv_rn(__dadd_rn(eu[k], __dmul_rn(lu[k], E.f_moon)), E.pl_cau);
+        if (k == 0) { P.x[AG_EAR] = xe; P.x[AG_MOO] = xm; }
+        else if (k == 1) { P.y[AG_EAR] = xe; P.y[AG_MOO] = xm; }
+        else { P.z[AG_EAR] = xe; P.z[AG_MOO] = xm; }
+        if (vel_em) {
+            const double ve = __ddiv_rn(__dadd_rn(ev[k], __dmul_rn(lv[k], E.f_earth)), E.cau_per_day);
+            const double vm = __ddiv_rn(__dadd_rn(ev[k], __dmul_rn(lv[k], E.f_moon)), E.cau_per_day);
+            if (k == 0) { P.vx[AG_EAR] = ve; P.vx[AG_MOO] = vm; }
+            else if (k == 1) { P.vy[AG_EAR] = ve; P.vy[AG_MOO] = vm; }
+            else { P.vz[AG_EAR] = ve; P.vz[AG_MOO] = vm; }
+        }
     }
     if (earth_acc) {
         double e_[10];

@@ -41,6 +41,8 @@ struct ascii_s {
     double mass[ASSIST_BODY_NPLANETS];
     double J2E, J3E, J4E, J2SUN, AU, RE, CLIGHT, ASUN;
     double* d_data = nullptr;
+    DevEphem* d_view = nullptr;      /* device copy of the last view handed to kernels */
+    DevEphem h_view;                 /* host copy of *d_view */
     bool find(const char* name, double* out) const {
         char key[7] = "      ";
         for (int i = 0; i < 6 && name[i]; i++) key[i] = name[i];
@@ -60,11 +62,11 @@ struct spk_s {
     std::vector<spk_target_h> targets;
     std::vector<double> data;
     std::vector<AgSpkSeg> segs;
-    std::vector<double2> meta;
+    std::vector<double4> meta;
     std::vector<int> seg0;
     double* d_data = nullptr;
     AgSpkSeg* d_segs = nullptr;
-    double2* d_meta = nullptr;
+    double4* d_meta = nullptr;
 };
 
 static bool read_file(const char* path, std::vector<unsigned char>& out) {
@@ -137,6 +139,7 @@ static ascii_s* ascii_load(const char* path) {
     std::vector<unsigned char> b;
     if (!read_file(path, b) || b.size() < 0x0B28 + 24) return nullptr;
     ascii_s* a = new ascii_s();
+    std::memset(&a->h_view, 0, sizeof(a->h_view));
     size_t o = 0x0A5C;
     a->beg = get<double>(b, o); a->end = get<double>(b, o + 8); a->inc = get<double>(b, o + 16);
     a->num = get<int32_t>(b, o + 24); a->cau = get<double>(b, o + 28); a->cem = get<double>(b, o + 36);
@@ -197,6 +200,7 @@ static ascii_s* ascii_load(const char* path) {
 static void ascii_free(ascii_s* a) {
     if (!a) return;
     if (a->d_data) cudaFree(a->d_data);
+    if (a->d_view) cudaFree(a->d_view);
     delete a;
 }
 
@@ -254,14 +258,17 @@ static spk_s* spk_load(const char* path) {
                 delete s; return nullptr;
             }
             g.init_jd = 2451545.0 + dir[-3] / 86400.0;
-            g.inv_intlen_days = 1.0 / (dir[-2] / 86400.0);
+            g.intlen_days = dir[-2] / 86400.0;
+            g.inv_intlen_days = 1.0 / g.intlen_days;
             g.data_off = one - 1;
             g.meta_off = (int)s->meta.size();
             for (int r = 0; r < g.nrec; r++) {
                 const double* val = s->data.data() + (one - 1) + (size_t)r * g.R;
-                double2 m;
+                double4 m;
                 m.x = 2451545.0 + val[0] / 86400.0;
-                m.y = 1.0 / (val[1] / 86400.0);
+                m.y = val[1] / 86400.0;
+                m.z = 1.0 / m.y;
+                m.w = 0.0;
                 s->meta.push_back(m);
             }
             s->segs.push_back(g);
@@ -271,8 +278,8 @@ static spk_s* spk_load(const char* path) {
               !ag_cuda_check(cudaMemcpy(s->d_data, s->data.data(), s->data.size() * 8, cudaMemcpyHostToDevice), "upload SPK") &&
               !ag_cuda_check(cudaMalloc(&s->d_segs, sizeof(AgSpkSeg) * (s->segs.size() + 1)), "cudaMalloc(SPK segments)") &&
               !ag_cuda_check(cudaMemcpy(s->d_segs, s->segs.data(), sizeof(AgSpkSeg) * s->segs.size(), cudaMemcpyHostToDevice), "upload segments") &&
-              !ag_cuda_check(cudaMalloc(&s->d_meta, sizeof(double2) * (s->meta.size() + 1)), "cudaMalloc(SPK records)") &&
-              !ag_cuda_check(cudaMemcpy(s->d_meta, s->meta.data(), sizeof(double2) * s->meta.size(), cudaMemcpyHostToDevice), "upload records");
+              !ag_cuda_check(cudaMalloc(&s->d_meta, sizeof(double4) * (s->meta.size() + 1)), "cudaMalloc(SPK records)") &&
+              !ag_cuda_check(cudaMemcpy(s->d_meta, s->meta.data(), sizeof(double4) * s->meta.size(), cudaMemcpyHostToDevice), "upload records");
     if (!ok) {
         if (s->d_data) cudaFree(s->d_data);
         if (s->d_segs) cudaFree(s->d_segs);
@@ -309,6 +316,9 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     }
     for (int k = 0; k < ASSIST_BODY_NPLANETS; k++) D.gm[k] = a->mass[k];
     D.inv_cau = 1.0 / a->cau;
+    D.cau_per_day = a->cau / 86400.;
+    D.f_earth = -1.0 / (1.0 + a->cem);
+    D.f_moon = a->cem / (1.0 + a->cem);
     const double l2 = std::log2(a->inc);
     D.pl_inc_pow2 = (a->inc > 0 && std::floor(l2) == l2) ? 1 : 0;
     D.pl_inv_inc = 1.0 / a->inc;
@@ -330,9 +340,21 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     }
     D.J2E = e->J2E; D.J3E = e->J3E; D.J4E = e->J4E; D.J2SUN = e->J2SUN;
     D.Re_eq = e->Re_eq; D.Rs_eq = e->Rs_eq; D.c_squared = e->c_squared; D.over_c_squared = e->over_c_squared;
+    ascii_s* am = e->ascii_planets;
+    if (!am->d_view && ag_cuda_check(cudaMalloc(&am->d_view, sizeof(DevEphem)), "cudaMalloc(ephemeris view)"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    D.self_dev = am->d_view;
+    if (std::memcmp(&am->h_view, &D, sizeof(D)) != 0) {
+        /* the view changed (first use, jd_ref or constants edited): refresh the device copy */
+        if (ag_cuda_check(cudaMemcpy(am->d_view, &D, sizeof(D), cudaMemcpyHostToDevice), "upload ephemeris view"))
+            return ASSIST_ERROR_EPHEM_FILE;
+        am->h_view = D;
+    }
     *out = D;
     return ASSIST_SUCCESS;
 }
+
+double ag_sun_gm(const struct assist_ephem* e) { return e->ascii_planets->mass[ASSIST_BODY_SUN]; }
 
 int ag_ephem_n_bodies(const struct assist_ephem* e) {
     return ASSIST_BODY_NPLANETS + (e && e->spk_asteroids ? (int)e->spk_asteroids->targets.size() : 0);

@@ -43,6 +43,10 @@ struct AgBatchArgs {
     double epsilon, min_dt, dt0;
     long long max_steps;
     long long watchdog_cycles;      /* per-thread clock64 budget; 0 = none */
+    /* warp-synchronous groups (K4g): group g = order[grp_start[g] .. + grp_size[g]) */
+    const int* grp_start;
+    const int* grp_size;
+    int n_groups;
 };
 
 /* launchers (kernels_forces.cu, kernels_ias15.cu) */
@@ -54,6 +58,8 @@ int ag_launch_bodies(const DevEphem& E, int n, const double* t, double* out, int
 size_t ag_batch_ws_doubles(int nslots, int nv);
 int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int tpb, cudaStream_t s);
 int ag_batch_max_slots(int nv, int tpb);
+int ag_group_max_slots(int nv);
+int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
 double ag_fp64_probe_gflops(void);
 
 /* shared-step device IAS15 (kernels_shared.cu) */

@@ -40,28 +40,14 @@ __device__ void ag_block_table(const DevEphem& E, const ForceCfg& c, double t, A
     if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
     if (s_st == AG_OK && tid < AG_NPL) {
         const int b = tid;
-        const double s = E.inv_cau;
-        double u[3], v[3];
-        const bool vel = (b == AG_SUN) || (b < nv);
-        if (b == AG_EAR || b == AG_MOO) {
-            double eu[3], ev[3], lu[3], lv[3];
-            if (vel) { ag_column<true>(E, s_rec, AG_C_EMB, s_tf, eu, ev); ag_column<true>(E, s_rec, AG_C_LUN, s_tf, lu, lv); }
-            else { ag_column<false>(E, s_rec, AG_C_EMB, s_tf, eu, ev); ag_column<false>(E, s_rec, AG_C_LUN, s_tf, lu, lv); }
-            const double f = b == AG_EAR ? -1.0 / (1.0 + E.pl_cem) : E.pl_cem / (1.0 + E.pl_cem);
-            for (int k = 0; k < 3; k++) { u[k] = fma(lu[k], f, eu[k]); v[k] = fma(lv[k], f, ev[k]); }
-        } else if (vel) {
-            ag_column<true>(E, s_rec, ag_col_of(b), s_tf, u, v);
-        } else {
-            ag_column<false>(E, s_rec, ag_col_of(b), s_tf, u, v);
-            v[0] = v[1] = v[2] = 0.0;
-        }
-        T.P.x[b] = u[0] * s; T.P.y[b] = u[1] * s; T.P.z[b] = u[2] * s;
+        double u[3], v[3] = {0.0, 0.0, 0.0};
+        if ((b == AG_SUN) || (b < nv)) ag_planet_exact<true>(E, s_rec, s_tf, b, u, v);
+        else ag_planet_exact<false>(E, s_rec, s_tf, b, u, v);
+        T.P.x[b] = u[0]; T.P.y[b] = u[1]; T.P.z[b] = u[2];
         T.P.vx[b] = v[0]; T.P.vy[b] = v[1]; T.P.vz[b] = v[2];
         if (b == AG_EAR && c.geocentric == 1) {
             double e_[10];
             ag_planet_full(E, AG_EAR, t, e_);
-            T.P.x[b] = e_[1]; T.P.y[b] = e_[2]; T.P.z[b] = e_[3];
-            T.P.vx[b] = e_[4]; T.P.vy[b] = e_[5]; T.P.vz[b] = e_[6];
             T.P.ex_a[0] = e_[7]; T.P.ex_a[1] = e_[8]; T.P.ex_a[2] = e_[9];
         }
     }
@@ -71,8 +57,9 @@ __device__ void ag_block_table(const DevEphem& E, const ForceCfg& c, double t, A
         if (tid >= 32 && tid - 32 < E.n_ast) {
             const int m = tid - 32;
             double h[3];
-            int st = ag_asteroid_pos(E, m, t, h);
-            T.ast[m][0] = h[0] + T.P.x[AG_SUN]; T.ast[m][1] = h[1] + T.P.y[AG_SUN]; T.ast[m][2] = h[2] + T.P.z[AG_SUN];
+            int st = ag_asteroid_exact(E, m, t, h);
+            T.ast[m][0] = __dadd_rn(h[0], T.P.x[AG_SUN]); T.ast[m][1] = __dadd_rn(h[1], T.P.y[AG_SUN]);
+            T.ast[m][2] = __dadd_rn(h[2], T.P.z[AG_SUN]);
             if (st != AG_OK && (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST))) atomicMax(&T.status, st);
         }
         if ((c.forces & AG_F_EIH) && tid < c.gr_eih_sources && tid < AG_NPL) {
@@ -97,7 +84,8 @@ __device__ __forceinline__ void ag_apply_jac(const double (*J)[6], const double 
 }
 
 /* All particles at one time.  Particle arrays are SoA (x[3][n]). */
-__global__ void __launch_bounds__(128) ag_k_forces_table(DevEphem E, ForceCfg c, double t, AgForceIO io) {
+__global__ void __launch_bounds__(128) ag_k_forces_table(const DevEphem* __restrict__ Ep, ForceCfg c, double t, AgForceIO io) {
+    const DevEphem& E = *Ep;
     __shared__ AgTable T;
     ag_block_table(E, c, t, T);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,10 +131,11 @@ __global__ void __launch_bounds__(128) ag_k_forces_table(DevEphem E, ForceCfg c,
 /* Every particle at its own time; nv (0 or 6) variational particles per real
  * particle stored right after it: state arrays are [n][6], var [n][nv][6]. */
 template <int NV>
-__global__ void __launch_bounds__(128) ag_k_forces_each(DevEphem E, ForceCfg c, int n, const double* __restrict__ t,
+__global__ void __launch_bounds__(128) ag_k_forces_each(const DevEphem* __restrict__ Ep, ForceCfg c, int n, const double* __restrict__ t,
                                                         const double* __restrict__ state, const double* __restrict__ params,
                                                         const double* __restrict__ var_state, double* __restrict__ acc,
                                                         double* __restrict__ var_acc, int* __restrict__ status) {
+    const DevEphem& E = *Ep;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double x[3] = {state[6 * (size_t)i], state[6 * (size_t)i + 1], state[6 * (size_t)i + 2]};
@@ -177,8 +166,9 @@ __global__ void __launch_bounds__(128) ag_k_forces_each(DevEphem E, ForceCfg c, 
 }
 
 /* Full body states: out[(ti * nb + b) * 10 + ...] = GM, x, y, z, vx, vy, vz, ax, ay, az. */
-__global__ void ag_k_bodies(DevEphem E, int n, const double* __restrict__ t, double* __restrict__ out,
+__global__ void ag_k_bodies(const DevEphem* __restrict__ Ep, int n, const double* __restrict__ t, double* __restrict__ out,
                             int* __restrict__ status) {
+    const DevEphem& E = *Ep;
     const int nb = AG_NPL + E.n_ast;
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n * nb) return;
@@ -191,9 +181,9 @@ __global__ void ag_k_bodies(DevEphem E, int n, const double* __restrict__ t, dou
         const int m = b - AG_NPL;
         double h[3], sun[10];
         o[0] = E.ast_gm[m];
-        st = ag_asteroid_pos(E, m, t[ti], h);
+        st = ag_asteroid_exact(E, m, t[ti], h);
         if (st == AG_OK) st = ag_planet_full(E, AG_SUN, t[ti], sun);
-        o[1] = h[0] + sun[1]; o[2] = h[1] + sun[2]; o[3] = h[2] + sun[3];
+        o[1] = __dadd_rn(h[0], sun[1]); o[2] = __dadd_rn(h[1], sun[2]); o[3] = __dadd_rn(h[2], sun[3]);
         for (int k = 4; k < 10; k++) o[k] = __longlong_as_double(0x7ff8000000000000LL);
     }
     if (status) atomicMax(&status[ti], st);
@@ -205,7 +195,7 @@ int ag_launch_forces_table(const DevEphem& E, const ForceCfg& c, double t, const
     if (io.n_real <= 0) return 0;
     const int tpb = 128;
     const int blocks = (io.n_real + tpb - 1) / tpb;
-    ag_k_forces_table<<<blocks, tpb, 0, s>>>(E, c, t, io);
+    ag_k_forces_table<<<blocks, tpb, 0, s>>>(E.self_dev, c, t, io);
     return (int)cudaGetLastError();
 }
 
@@ -215,8 +205,8 @@ int ag_launch_forces_each(const DevEphem& E, const ForceCfg& c, int n, const dou
     if (n <= 0) return 0;
     const int tpb = 128;
     const int blocks = (n + tpb - 1) / tpb;
-    if (nv == 6) ag_k_forces_each<6><<<blocks, tpb, 0, s>>>(E, c, n, t, state, params, var_state, acc, var_acc, status);
-    else ag_k_forces_each<0><<<blocks, tpb, 0, s>>>(E, c, n, t, state, params, var_state, acc, var_acc, status);
+    if (nv == 6) ag_k_forces_each<6><<<blocks, tpb, 0, s>>>(E.self_dev, c, n, t, state, params, var_state, acc, var_acc, status);
+    else ag_k_forces_each<0><<<blocks, tpb, 0, s>>>(E.self_dev, c, n, t, state, params, var_state, acc, var_acc, status);
     return (int)cudaGetLastError();
 }
 
@@ -224,6 +214,6 @@ int ag_launch_bodies(const DevEphem& E, int n, const double* t, double* out, int
     const int nb = AG_NPL + E.n_ast;
     const int total = n * nb;
     if (total <= 0) return 0;
-    ag_k_bodies<<<(total + 127) / 128, 128, 0, s>>>(E, n, t, out, status);
+    ag_k_bodies<<<(total + 127) / 128, 128, 0, s>>>(E.self_dev, n, t, out, status);
     return (int)cudaGetLastError();
 }

@@ -135,7 +135,8 @@ __device__ __forceinline__ void ag_predict_next(const Ws<C>& W, double ratio) {
 }
 
 template <int NV>
-__global__ void __launch_bounds__(128) ag_k_batch(DevEphem E, ForceCfg cf, AgBatchArgs A) {
+__global__ void __launch_bounds__(128) ag_k_batch(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
+    const DevEphem& E = *Ep;
     constexpr int C = 3 * (1 + NV);
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= A.nslots) return;
@@ -422,8 +423,8 @@ int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, 
     if (e) return e;
     if (tpb > 128) tpb = 128;
     const int blocks = (a.nslots + tpb - 1) / tpb;
-    if (nv == 6) ag_k_batch<6><<<blocks, tpb, 0, s>>>(E, c, a);
-    else ag_k_batch<0><<<blocks, tpb, 0, s>>>(E, c, a);
+    if (nv == 6) ag_k_batch<6><<<blocks, tpb, 0, s>>>(E.self_dev, c, a);
+    else ag_k_batch<0><<<blocks, tpb, 0, s>>>(E.self_dev, c, a);
     return (int)cudaGetLastError();
 }
 
@@ -474,4 +475,391 @@ extern "C" int ag_debug_ias_tables(double* out) {
     int e = ag_ias_tables_init();
     if (e) return e;
     return (int)cudaMemcpyFromSymbol(out, ag_ias, sizeof(IasTables));
+}
+
+/* =========================================================================
+ * K4g: warp-synchronous groups.
+ *
+ * A warp integrates a group of up to 32 particles that start at the same t0
+ * (the host groups particles by start time, direction, orbital timescale
+ * q^1.5 and integration length).  The group shares t and the adaptive step:
+ * each lane runs IAS15's own error control for its particle and the group
+ * takes the most restrictive step (dt = min over lanes, rejection when any
+ * lane rejects); predictor-corrector iterations continue until every lane has
+ * converged (a converged lane keeps its b).  Sharing the time lets the warp
+ * evaluate every body ONCE per node, one lane per planet / asteroid, with the
+ * reference's exact arithmetic, into a per-warp table in shared memory that
+ * all 32 lanes read; per-lane FP64 work is then the force model alone.  A
+ * lane whose particle reaches its own t_end writes it back and idles until
+ * the group is done; the warp then takes the next group from the queue
+ * (groups ordered longest first).
+ * ========================================================================= */
+
+#define AG_FULL 0xffffffffu
+
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(AG_FULL, v, o));
+    return v;
+}
+
+/* The body table for time t, built by the whole warp (uniform result). */
+__device__ int ag_warp_table(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
+    const double* rec = nullptr;
+    double tf = 0.0;
+    int st = ag_planet_record(E, t, &rec, &tf);
+    if (st != AG_OK) return st;
+    int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
+    if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
+    if (lane < AG_NPL) {
+        double u[3], v[3] = {0.0, 0.0, 0.0};
+        if (lane == AG_SUN || lane < nv) ag_planet_exact<true>(E, rec, tf, lane, u, v);
+        else ag_planet_exact<false>(E, rec, tf, lane, u, v);
+        T.P.x[lane] = u[0]; T.P.y[lane] = u[1]; T.P.z[lane] = u[2];
+        T.P.vx[lane] = v[0]; T.P.vy[lane] = v[1]; T.P.vz[lane] = v[2];
+        if (lane == AG_EAR && c.geocentric == 1) {
+            double e_[10];
+            ag_planet_full(E, AG_EAR, t, e_);
+            T.P.ex_a[0] = e_[7]; T.P.ex_a[1] = e_[8]; T.P.ex_a[2] = e_[9];
+        }
+    }
+    __syncwarp();
+    int ast_st = AG_OK;
+    if (lane >= AG_NPL)
+        for (int m = lane - AG_NPL; m < E.n_ast; m += 32 - AG_NPL) {
+            double h[3];
+            const int s2 = ag_asteroid_exact(E, m, t, h);
+            if (s2 != AG_OK) ast_st = s2;
+            T.ast[m][0] = __dadd_rn(h[0], T.P.x[AG_SUN]);
+            T.ast[m][1] = __dadd_rn(h[1], T.P.y[AG_SUN]);
+            T.ast[m][2] = __dadd_rn(h[2], T.P.z[AG_SUN]);
+        }
+    if ((c.forces & AG_F_EIH) && lane < c.gr_eih_sources && lane < AG_NPL) {
+        double aj[3], t1;
+        ag_eih_source(E, T.P, lane, aj, &t1);
+        T.eih_a[lane][0] = aj[0]; T.eih_a[lane][1] = aj[1]; T.eih_a[lane][2] = aj[2]; T.eih_t1[lane] = t1;
+    }
+    if (!(c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST))) ast_st = AG_OK;
+    __syncwarp();
+    const unsigned bad = __ballot_sync(AG_FULL, ast_st != AG_OK);
+    T.status = AG_OK;
+    return bad ? AG_ERR_COVERAGE : AG_OK;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
+    constexpr int C = 3 * (1 + NV);
+    const DevEphem& E = *Ep;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    __shared__ AgTable tabs[4];
+    AgTable& Tab = tabs[wib];
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const Ws<C> W{A.ws, A.nslots, slot};
+    const long long clk0 = clock64();
+    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0;
+    bool stop = false;
+
+    while (!stop) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(A.queue, 1);
+        g = __shfl_sync(AG_FULL, g, 0);
+        if (g >= A.n_groups) break;
+        const int gs = A.grp_size[g], g0 = A.grp_start[g];
+        const int pid = lane < gs ? A.order[g0 + lane] : -1;
+        double t = A.t0[A.order[g0]], tc = 0.0, dtls = 0.0;
+        const double tend = pid >= 0 ? A.t_end[pid] : t;
+        double dir = 0.0;
+        {
+            double d = pid >= 0 ? (tend - t) : 0.0;
+            const unsigned fwd = __ballot_sync(AG_FULL, d > 0.0), bwd = __ballot_sync(AG_FULL, d < 0.0);
+            dir = fwd ? 1.0 : (bwd ? -1.0 : 1.0);
+        }
+        double dt = dir * fabs(A.dt0);
+        double prm[3] = {0.0, 0.0, 0.0};
+        bool has_prm = false;
+        int pstat = AG_ST_OK;
+        bool live = pid >= 0;
+        if (live) {
+            const double* s0 = A.state + 6 * (size_t)pid;
+            for (int k = 0; k < 3; k++) { W(W_X0, k) = s0[k]; W(W_V0, k) = s0[3 + k]; W(W_XC, k) = 0.0; W(W_VC, k) = 0.0; }
+            for (int q = 0; q < NV; q++) {
+                const double* vs = A.var_state + ((size_t)pid * NV + q) * 6;
+                for (int k = 0; k < 3; k++) {
+                    W(W_X0, 3 + 3 * q + k) = vs[k]; W(W_V0, 3 + 3 * q + k) = vs[3 + k];
+                    W(W_XC, 3 + 3 * q + k) = 0.0; W(W_VC, 3 + 3 * q + k) = 0.0;
+                }
+            }
+            for (int comp = 0; comp < C; comp++)
+                for (int k = 0; k < 7; k++) {
+                    W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; W(W_BR + k, comp) = 0.0; W(W_ER + k, comp) = 0.0;
+                }
+            if (A.params) {
+                prm[0] = A.params[3 * (size_t)pid]; prm[1] = A.params[3 * (size_t)pid + 1]; prm[2] = A.params[3 * (size_t)pid + 2];
+                has_prm = true;
+            }
+        }
+        bool finish_now = live && (tend == t);
+        long long steps = 0;
+        while (true) {
+            /* ---- retire lanes whose particle is complete */
+            if (finish_now) {
+                double* s0 = A.state + 6 * (size_t)pid;
+                bool finite = true;
+                for (int k = 0; k < 3; k++) {
+                    s0[k] = W(W_X0, k) + W(W_XC, k);
+                    s0[3 + k] = W(W_V0, k) + W(W_VC, k);
+                    finite = finite && isfinite(s0[k]) && isfinite(s0[3 + k]);
+                }
+                for (int q = 0; q < NV; q++) {
+                    double* vs = A.var_state + ((size_t)pid * NV + q) * 6;
+                    for (int k = 0; k < 3; k++) {
+                        vs[k] = W(W_X0, 3 + 3 * q + k) + W(W_XC, 3 + 3 * q + k);
+                        vs[3 + k] = W(W_V0, 3 + 3 * q + k) + W(W_VC, 3 + 3 * q + k);
+                    }
+                }
+                if (pstat == AG_ST_OK && !finite) pstat = AG_ST_NONFINITE;
+                if (A.status) A.status[pid] = pstat;
+                live = false;
+                finish_now = false;
+            }
+            if (!__any_sync(AG_FULL, live)) break;
+            if (A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles) {
+                pstat = AG_ST_TIMEOUT;
+                finish_now = live;
+                stop = true;
+                continue;
+            }
+            /* ---- step size: no further than the nearest unfinished end */
+            const double rem = live ? fabs((tend - t) - tc) : 1e300;
+            const double rem_min = warp_min(rem);
+            double hstep;
+            bool last_group = false;
+            if (fabs(dt) >= rem_min) { hstep = dir * rem_min; last_group = true; }
+            else hstep = dt;
+            const bool last = live && last_group && rem == rem_min;
+            /* ---- node 0: accelerations at the step start, g from the predicted b */
+            int st = ag_warp_table(E, cf, t, Tab, lane);
+            if (st != AG_OK) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            if (live) {
+                double at[C];
+                double xp[3] = {W(W_X0, 0), W(W_X0, 1), W(W_X0, 2)}, vp[3] = {W(W_V0, 0), W(W_V0, 1), W(W_V0, 2)};
+                TableBodies B(Tab);
+                if (NV > 0) {
+                    double J[3][6], JA[3][3];
+                    bool has_ng;
+                    st = ag_forces<TableBodies, true>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, J, JA, &has_ng);
+                    for (int q = 0; q < NV; q++)
+                        for (int a = 0; a < 3; a++) {
+                            double s = 0.0;
+                            for (int b = 0; b < 3; b++) {
+                                s = fma(J[a][b], W(W_X0, 3 + 3 * q + b), s);
+                                s = fma(J[a][3 + b], W(W_V0, 3 + 3 * q + b), s);
+                            }
+                            at[3 + 3 * q + a] = s;
+                        }
+                } else {
+                    st = ag_forces<TableBodies, false>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, nullptr, nullptr, nullptr);
+                }
+                n_ev++;
+                for (int comp = 0; comp < C; comp++) {
+                    W(W_A0, comp) = at[comp];
+                    double b[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+#pragma unroll
+                    for (int j = 0; j < 7; j++) {
+                        double s = b[j];
+#pragma unroll
+                        for (int k = j + 1; k < 7; k++) s = fma(b[k], ag_ias.d[j][k], s);
+                        W(W_G + j, comp) = s;
+                    }
+                }
+            }
+            /* ---- predictor-corrector iterations */
+            int iters = 1;
+            double pc_last = 1e300, ma7 = 0.0;
+            bool conv = !live;
+            while (true) {
+                for (int n = 1; n < 8; n++) {
+                    const double hn = ag_ias.h[n];
+                    const double tn = t + (tc + hstep * hn);
+                    st = ag_warp_table(E, cf, tn, Tab, lane);
+                    if (st != AG_OK) break;
+                    if (!conv) {
+                        double sx[9], sv[8];
+                        sx[0] = hstep * hn;
+                        sx[1] = sx[0] * sx[0] * 0.5;
+#pragma unroll
+                        for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * ag_ias.fx[n][k];
+                        sv[0] = hstep * hn;
+#pragma unroll
+                        for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * ag_ias.fv[n][k];
+                        double xp[C], vp[C];
+                        for (int comp = 0; comp < C; comp++) {
+                            double px = sx[8] * W(W_B + 6, comp);
+#pragma unroll
+                            for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, comp), px);
+                            px = fma(sx[1], W(W_A0, comp), px);
+                            px = fma(sx[0], W(W_V0, comp), px);
+                            xp[comp] = W(W_X0, comp) + (px + W(W_XC, comp));
+                            double pv = sv[7] * W(W_B + 6, comp);
+#pragma unroll
+                            for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(W_B + j, comp), pv);
+                            pv = fma(sv[0], W(W_A0, comp), pv);
+                            vp[comp] = W(W_V0, comp) + (pv + W(W_VC, comp));
+                        }
+                        double at[C];
+                        TableBodies B(Tab);
+                        if (NV > 0) {
+                            double J[3][6], JA[3][3];
+                            bool has_ng;
+                            ag_forces<TableBodies, true>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, J, JA, &has_ng);
+                            for (int q = 0; q < NV; q++)
+                                for (int a = 0; a < 3; a++) {
+                                    double s = 0.0;
+                                    for (int b = 0; b < 3; b++) {
+                                        s = fma(J[a][b], xp[3 + 3 * q + b], s);
+                                        s = fma(J[a][3 + b], vp[3 + 3 * q + b], s);
+                                    }
+                                    at[3 + 3 * q + a] = s;
+                                }
+                        } else {
+                            ag_forces<TableBodies, false>(B, E, cf, xp, vp, has_prm ? prm : nullptr, at, nullptr, nullptr, nullptr);
+                        }
+                        n_ev++;
+                        double maxa = 0.0, maxdb = 0.0;
+                        for (int comp = 0; comp < C; comp++) {
+                            double gn = (at[comp] - W(W_A0, comp)) * ag_ias.rrinv[n][0];
+                            for (int j = 1; j < n; j++) gn = (gn - W(W_G + j - 1, comp)) * ag_ias.rrinv[n][j];
+                            const double delta = gn - W(W_G + n - 1, comp);
+                            W(W_G + n - 1, comp) = gn;
+                            for (int k = 0; k < n - 1; k++) W(W_B + k, comp) = fma(delta, ag_ias.c[n - 1][k], W(W_B + k, comp));
+                            W(W_B + n - 1, comp) += delta;
+                            if (n == 7 && comp < 3) {
+                                const double aa = fabs(at[comp]);
+                                if (ag_isnormal_pos(aa) && aa > maxa) maxa = aa;
+                                const double db = fabs(delta);
+                                if (ag_isnormal_pos(db) && db > maxdb) maxdb = db;
+                            }
+                        }
+                        if (n == 7) {
+                            ma7 = maxa;
+                            const double pc_err = maxdb / maxa;
+                            conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+                            if (conv) n_it += (unsigned long long)iters;
+                            else pc_last = pc_err;
+                        }
+                    }
+                }
+                if (st != AG_OK) break;
+                if (__all_sync(AG_FULL, conv)) break;
+                iters++;
+            }
+            if (st != AG_OK) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            /* ---- step-size control: each lane's choice, the group takes the smallest */
+            double dt_new_l = 1e300, dt_nocap_l = 1e300;
+            bool rej_l = false;
+            if (A.epsilon > 0.0 && live) {
+                double mb = 0.0;
+                for (int k = 0; k < 3; k++) {
+                    const double bb = fabs(W(W_B + 6, k));
+                    if (ag_isnormal_pos(bb) && bb > mb) mb = bb;
+                }
+                const double err = mb / ma7;
+                const double safety = 0.25;
+                double dn;
+                if (ag_isnormal_pos(err)) dn = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
+                else dn = hstep / safety;
+                if (fabs(dn) < A.min_dt) dn = copysign(A.min_dt, dn);
+                dt_nocap_l = fabs(dn);
+                const double ratio = dn / hstep;
+                if (fabs(ratio) < safety) rej_l = true;
+                else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
+                dt_new_l = fabs(dn);
+            }
+            double dt_new;
+            if (A.epsilon > 0.0) {
+                dt_new = dir * warp_min(dt_new_l);
+                /* a step shortened to land on a lane's t_end does not shrink the
+                 * group's step beyond what the error control asks for */
+                if (last_group) dt_new = dir * fmin(fabs(dt), fmax(fabs(dt_new), warp_min(dt_nocap_l)));
+            } else {
+                dt_new = dt;            /* fixed step */
+            }
+            const bool reject = __any_sync(AG_FULL, rej_l);
+            if (reject) {
+                n_rej += live ? 1 : 0;
+                if (live) {
+                    if (dtls != 0.0) ag_predict_next<C>(W, dt_new / dtls);
+                    else
+                        for (int comp = 0; comp < C; comp++)
+                            for (int k = 0; k < 7; k++) { W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; }
+                }
+                dt = dt_new;
+                continue;
+            }
+            /* ---- accept */
+            if (live) {
+                n_acc++;
+                const double h2 = hstep * hstep;
+                for (int comp = 0; comp < C; comp++) {
+                    double b[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+                    const double a0 = W(W_A0, comp);
+                    double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
+                    ix = fma(ix, h2, W(W_V0, comp) * hstep);
+                    double y = ix + W(W_XC, comp);
+                    const double x0 = W(W_X0, comp);
+                    double s = x0 + y;
+                    W(W_XC, comp) = y - (s - x0);
+                    W(W_X0, comp) = s;
+                    double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
+                    iv = iv * hstep;
+                    y = iv + W(W_VC, comp);
+                    const double v0 = W(W_V0, comp);
+                    s = v0 + y;
+                    W(W_VC, comp) = y - (s - v0);
+                    W(W_V0, comp) = s;
+#pragma unroll
+                    for (int k = 0; k < 7; k++) { W(W_ER + k, comp) = W(W_E + k, comp); W(W_BR + k, comp) = b[k]; }
+                }
+                ag_predict_next<C>(W, dt_new / hstep);
+            }
+            {
+                const double y = hstep + tc;
+                const double s = t + y;
+                tc = y - (s - t);
+                t = s;
+            }
+            dtls = hstep;
+            dt = dt_new;
+            steps++;
+            if (last) finish_now = true;
+            if (last_group && live && !last && fabs((tend - t) - tc) == 0.0) finish_now = true;
+            if (A.max_steps > 0 && steps >= A.max_steps && live && !finish_now) { pstat = AG_ST_BUDGET; finish_now = true; }
+        }
+    }
+    atomicAdd(&A.counters[0], n_acc);
+    atomicAdd(&A.counters[1], n_rej);
+    atomicAdd(&A.counters[2], n_ev);
+    atomicAdd(&A.counters[3], n_it);
+}
+
+int ag_group_max_slots(int nv) {
+    int dev = 0, sms = 0, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (nv == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_group<6>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_group<0>, 128, 0);
+    if (bps < 1) bps = 1;
+    return sms * bps * 128;
+}
+
+int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s) {
+    int e = ag_ias_tables_init();
+    if (e) return e;
+    const int blocks = (a.nslots + 127) / 128;
+    if (nv == 6) ag_k_group<6><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+    else ag_k_group<0><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+    return (int)cudaGetLastError();
 }

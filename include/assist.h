@@ -203,6 +203,9 @@ struct assist_gb300_options {
     int max_steps;          /* per-particle step budget, 0 => unlimited */
     int warm_start;         /* 0 plain predictor, 1 learned warm start (needs a loaded MLP) */
     int threads_per_block;  /* 0 => autotuned */
+    int group_steps;        /* 1 (default): up to 32 particles with the same start time and
+                               similar orbital timescale share each adaptive step (one warp);
+                               0: every particle takes its own adaptive step */
 };
 
 /* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */

@@ -44,7 +44,8 @@ class Options(ctypes.Structure):
     _fields_ = [("forces", c_int), ("gr_eih_sources", c_int), ("geocentric", c_int),
                 ("alpha", c_double), ("nk", c_double), ("nm", c_double), ("nn", c_double), ("r0", c_double),
                 ("epsilon", c_double), ("min_dt", c_double), ("dt0", c_double), ("max_steps", c_int),
-                ("warm_start", c_int), ("threads_per_block", c_int), ("group_steps", c_int)]
+                ("warm_start", c_int), ("threads_per_block", c_int), ("group_steps", c_int),
+                ("dt_floor", c_double)]
 
 
 class BatchStats(ctypes.Structure):

@@ -535,6 +535,7 @@ extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
     o->warm_start = 0;
     o->threads_per_block = 0;
     o->group_steps = 1;
+    o->dt_floor = 1e-8;
 }
 
 extern "C" int assist_gb300_n_bodies(const struct assist_ephem* e) { return ag_ephem_n_bodies(e); }
@@ -726,6 +727,7 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
     a.status = d_status; a.ws = g_batch.d_ws; a.counters = g_batch.d_counters;
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
+    a.dt_floor = o->dt_floor;
     if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
     /* per-thread run-time budget: ASSIST_GB300_WATCHDOG_S seconds (default 300) at the boost clock */
     double wd = 300.0;

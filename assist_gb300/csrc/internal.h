@@ -40,7 +40,7 @@ struct AgBatchArgs {
     int* status;                    /* [n] or null */
     double* ws;                     /* per-slot workspace, see kernels_ias15.cu */
     unsigned long long* counters;   /* accepted, rejected, evals, iterations, warm used, warm fallback */
-    double epsilon, min_dt, dt0;
+    double epsilon, min_dt, dt0, dt_floor;
     long long max_steps;
     long long watchdog_cycles;      /* per-thread clock64 budget; 0 = none */
     /* warp-synchronous groups (K4g): group g = order[grp_start[g] .. + grp_size[g]) */

@@ -42,6 +42,7 @@
 #define AG_ST_COVERAGE 1
 #define AG_ST_NONFINITE 2
 #define AG_ST_BUDGET 3
+#define AG_ST_UNDERFLOW 4
 #define AG_ST_TIMEOUT 5
 
 struct IasTables {
@@ -326,7 +327,11 @@ __global__ void __launch_bounds__(128) ag_k_batch(const DevEphem* __restrict__ E
                             if (fabs(ratio) < safety) reject = true;
                             else if (fabs(ratio) > 1.0 / safety) dt_new = hstep / safety;
                         }
-                        if (reject) {
+                        if (A.dt_floor > 0.0 && fabs(dt_new) < A.dt_floor) {
+                            /* step underflow: the particle is hitting a body */
+                            pstat = AG_ST_UNDERFLOW;
+                            phase = 3;
+                        } else if (reject) {
                             n_rej++;
                             if (dtls != 0.0) ag_predict_next<C>(W, dt_new / dtls);
                             else
@@ -775,6 +780,18 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
                 if (fabs(ratio) < safety) rej_l = true;
                 else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
                 dt_new_l = fabs(dn);
+            }
+            if (live && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
+                /* step underflow: this lane's particle is hitting a body; it stops
+                 * (state of the step start) and the group goes on without it */
+                pstat = AG_ST_UNDERFLOW;
+                finish_now = true;
+                rej_l = false;
+                dt_new_l = 1e300;
+                dt_nocap_l = 1e300;
+            }
+            if (__any_sync(AG_FULL, finish_now && pstat == AG_ST_UNDERFLOW)) {
+                if (!__any_sync(AG_FULL, live && !finish_now)) continue;   /* only underflowing lanes left */
             }
             double dt_new;
             if (A.epsilon > 0.0) {

@@ -131,9 +131,10 @@ def cpu_baseline(pl, ast, pop, target_s: float = 15.0, threads=None):
     n = int(min(pop.t0.size, max(n_pilot, n_pilot * target_s / max(pilot, 1e-3))))
     idx = rng.choice(pop.t0.size, size=n, replace=False)
     t = time.perf_counter()
-    o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx], threads=threads)
+    _, _, st, _ = o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx],
+                                    threads=threads, return_all=True)
     dt = time.perf_counter() - t
-    pdays = float(np.abs(pop.t_end[idx] - pop.t0[idx]).sum())
+    pdays = float(np.abs(pop.t_end[idx] - pop.t0[idx])[st == 0].sum())
     return {"value": pdays / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d of the %d particles (random, seed 7), their full integrations: %.3g particle-days in %.1f s"
                       % (n, pop.t0.size, pdays, dt)}
@@ -163,9 +164,10 @@ def run_reference(args):
     for _ in range(args.steps):
         idx = rng.choice(pop.t0.size, size=n, replace=False)
         t = time.perf_counter()
-        o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx], threads=threads)
+        _, _, st, _ = o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx],
+                                        threads=threads, return_all=True)
         tot_s += time.perf_counter() - t
-        tot_days += float(np.abs(pop.t_end[idx] - pop.t0[idx]).sum())
+        tot_days += float(np.abs(pop.t_end[idx] - pop.t0[idx])[st == 0].sum())
     v = tot_days / tot_s
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True,
@@ -247,11 +249,17 @@ def main():
     wall = time.perf_counter() - wall0
     clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in evs)
+    # particle-days of the particles that reached t_end (a particle that hits a
+    # body stops with status 4 and its span is not counted)
+    st_host = status.cpu().numpy()
+    done = st_host == 0
+    pdays = float(np.abs(pop.t_end - pop.t0)[done].sum())
     if world > 1:
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    bad = int((status != 0).sum().item())
+    bad = int((~done).sum())
+    status_counts = {str(k): int(v) for k, v in zip(*np.unique(st_host, return_counts=True))}
     value = world * pdays * args.steps / (ms / 1e3)
     # e2e through the host-array C entry point
     e2e = None
@@ -262,7 +270,7 @@ def main():
         e2e_s = time.perf_counter() - t
         h2d = pop.t0.nbytes * 2 + pop.state.nbytes + pop.params.nbytes
         d2h = pop.state.nbytes + hstat.nbytes
-        e2e = {"value": pdays / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        e2e = {"value": float(np.abs(pop.t_end - pop.t0)[hstat == 0].sum()) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -290,7 +298,7 @@ def main():
                       "force_evals": stats_acc["force_evals"] // args.steps,
                       "iterations_per_step": stats_acc["pc_iterations"] / max(stats_acc["steps_accepted"] +
                                                                               stats_acc["steps_rejected"], 1)},
-            "failed_particles": bad, "wall_s_timed_region": wall}
+            "unfinished_particles": bad, "status_counts": status_counts, "wall_s_timed_region": wall}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -206,6 +206,9 @@ struct assist_gb300_options {
     int group_steps;        /* 1 (default): up to 32 particles with the same start time and
                                similar orbital timescale share each adaptive step (one warp);
                                0: every particle takes its own adaptive step */
+    double dt_floor;        /* a particle whose adaptive step falls below this |dt| (days)
+                               stops with ASSIST_GB300_STEP_UNDERFLOW (an impact: any orbit
+                               outside a body needs steps > 1e-4 day); 0 disables */
 };
 
 /* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */
@@ -217,7 +220,8 @@ enum ASSIST_GB300_PARTICLE_STATUS {
     ASSIST_GB300_COVERAGE = 1,      /* a substep time fell outside the ephemeris */
     ASSIST_GB300_NONFINITE = 2,     /* NaN/Inf in state or acceleration */
     ASSIST_GB300_STEP_BUDGET = 3,   /* max_steps reached before t_end */
-    ASSIST_GB300_MIN_DT = 4,        /* informational: min_dt clamp was applied */
+    ASSIST_GB300_STEP_UNDERFLOW = 4,/* the adaptive step fell below dt_floor (impact) */
+    ASSIST_GB300_TIMEOUT = 5,       /* the kernel's run-time budget was spent */
 };
 
 /* Statistics returned by the batched integrator. */

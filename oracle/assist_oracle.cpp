@@ -306,6 +306,67 @@ static int ascii_body(const Ephem& e, T t, int body, T* out) {
     return OK;
 }
 
+/* As ascii_body, evaluating velocity and acceleration only when asked (the
+ * position sums are the same operations either way). */
+template <class T>
+static void cheb_column_need(const double* P, int ncm, int ncf, int niv, T tfrac, double inc, T* u, T* v, T* w,
+                             bool vel) {
+    if (vel) { cheb_column(P, ncm, ncf, niv, tfrac, inc, u, v, w); return; }
+    T Tp[32];
+    T tt = tfrac * (double)niv;
+    T fl = floor(tt);
+    T tau = 2.0 * (tt - fl) - 1.0;
+    int blk = (int)to_double(tt);
+    Tp[0] = 1.0; Tp[1] = tau;
+    for (int p = 2; p < ncf; p++) Tp[p] = 2.0 * tau * Tp[p - 1] - Tp[p - 2];
+    for (int m = 0; m < ncm; m++) {
+        T su = 0.0;
+        const double* cf = P + ncf * (m + blk * ncm);
+        for (int p = 0; p < ncf; p++) su += Tp[p] * cf[p];
+        u[m] = su;
+    }
+}
+
+template <class T>
+static int ascii_body_need(const Ephem& e, T t, int body, T* out, bool vel, bool acc) {
+    if (acc) return ascii_body(e, t, body, out);
+    const Ascii& a = *e.pl;
+    if (body < 0 || body >= NPL) return ERR_NEPHEM;
+    out[0] = a.mass[body];
+    double jd = to_double(T(e.jd_ref) + t);
+    if (jd < a.beg || jd > a.end) return ERR_COVERAGE;
+    uint32_t blk = (uint32_t)to_double((T(e.jd_ref) + t - a.beg) / a.inc);
+    size_t nrec = a.data.size() / a.rec;
+    if ((size_t)blk + 2 >= nrec) return ERR_COVERAGE;
+    const double* z = a.data.data() + (size_t)(blk + 2) * a.rec;
+    T tf = ((T(e.jd_ref) - a.beg - (double)blk * a.inc) + t) / a.inc;
+    static const int col_of[NPL] = {C_SUN, C_MER, C_VEN, -1, -1, C_MAR, C_JUP, C_SAT, C_URA, C_NEP, C_PLU};
+    T u[3], v[3], w[3];
+    if (body == B_EAR || body == B_MOO) {
+        T eu[3], ev[3], ew[3], lu[3], lv[3], lw[3];
+        cheb_column_need(z + a.off[C_EMB], 3, a.ncf[C_EMB], a.niv[C_EMB], tf, a.inc, eu, ev, ew, vel);
+        cheb_column_need(z + a.off[C_LUN], 3, a.ncf[C_LUN], a.niv[C_LUN], tf, a.inc, lu, lv, lw, vel);
+        double f = body == B_EAR ? -1.0 / (1.0 + a.cem) : a.cem / (1.0 + a.cem);
+        for (int k = 0; k < 3; k++) {
+            u[k] = eu[k] + lu[k] * f;
+            if (vel) { v[k] = ev[k] + lv[k] * f; w[k] = ew[k] + lw[k] * f; }
+        }
+    } else {
+        int c = col_of[body];
+        cheb_column_need(z + a.off[c], 3, a.ncf[c], a.niv[c], tf, a.inc, u, v, w, vel);
+    }
+    for (int k = 0; k < 3; k++) {
+        out[1 + k] = u[k] / a.cau;
+        if (vel) {
+            out[4 + k] = v[k] / (a.cau / 86400.);
+            out[7 + k] = w[k] / (a.cau / (86400. * 86400.));
+        } else {
+            out[4 + k] = NAN; out[7 + k] = NAN;
+        }
+    }
+    return OK;
+}
+
 /* Asteroid heliocentric position, src/spk.c:405-481 (AU fixed at 149597870.7 km). */
 template <class T>
 static int spk_position(const Ephem& e, T t, int m, T* gm, T* pos) {
@@ -358,6 +419,15 @@ static int body_state(const Ephem& e, int i, T t, T* out) {
 /* ---------------------------------------------------------------- forces */
 struct ForceOpts { int forces, gr_eih_sources, geocentric; double alpha, nk, nm, nn, r0; };
 
+/* Does the force model read body i's velocity?  The Sun's (non-grav, GR
+ * simple, EIH), the EIH sources' and, geocentric, the Earth's. */
+static bool need_velocity(const ForceOpts& o, int i) {
+    if (i == B_SUN) return true;
+    if ((o.forces & F_EIH) && i < o.gr_eih_sources) return true;
+    if (o.geocentric == 1 && i == B_EAR) return true;
+    return false;
+}
+
 /* Accelerations of n_real real particles (x, v: 3*n_real) and n_var first
  * order variational particles (vx, vv: 3*n_var; var k belongs to real
  * particle vtp[k], particle_params row n_real + k) at time t; acc receives
@@ -367,9 +437,24 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
                   int n_var, const int* vtp, const T* vx, const T* vv, const double* params, T* acc) {
     const int nb = NPL + e.n_ast();
     std::vector<T> B((size_t)nb * 10);
-    for (int i = 0; i < nb; i++) {
-        int f = body_state(e, i, t, &B[(size_t)i * 10]);
+    /* Body states at t.  The reference evaluates position, velocity and
+     * acceleration of every planet (src/ascii_ephem.c:27-65) and, for every
+     * asteroid, the Sun again (src/forces.c:216); positions do not depend on
+     * the velocity/acceleration sums, so evaluating each planet once, with
+     * only the derivatives the force model reads, gives identical values and
+     * an operation count without the reference's redundant work. */
+    for (int i = 0; i < NPL; i++) {
+        int f = ascii_body_need(e, t, i, &B[(size_t)i * 10], need_velocity(o, i), o.geocentric == 1 && i == B_EAR);
         if (f != OK) return f;
+    }
+    for (int i = NPL; i < nb; i++) {
+        T gm, p[3];
+        int f = spk_position(e, t, i - NPL, &gm, p);
+        if (f != OK) return f;
+        T* out = &B[(size_t)i * 10];
+        out[0] = gm;
+        out[1] = p[0] + B[1]; out[2] = p[1] + B[2]; out[3] = p[2] + B[3];
+        for (int k = 4; k < 10; k++) out[k] = NAN;
     }
     auto GM = [&](int i) { return B[(size_t)i * 10]; };
     auto BX = [&](int i, int k) { return B[(size_t)i * 10 + 1 + k]; };
@@ -882,7 +967,7 @@ static IasConst make_constants() {
 }
 static const IasConst& K() { static IasConst k = make_constants(); return k; }
 
-struct IasOpts { double epsilon, min_dt; int max_steps; int max_iter; };
+struct IasOpts { double epsilon, min_dt; int max_steps; int max_iter; double dt_floor; };
 struct IasStats { long long accepted, rejected, evals, iterations; int status; };
 
 template <class T>
@@ -1013,6 +1098,8 @@ struct Ias15 {
             if (std::isnormal(to_double(err))) dt_new = T(std::pow(o.epsilon / to_double(err), 1.0 / 7.0)) * dt_done;
             else dt_new = dt_done / safety;
             if (to_double(fabs(dt_new)) < o.min_dt) dt_new = T(std::copysign(o.min_dt, to_double(dt_new)));
+            /* step underflow (an impact): stop, keeping the state of the step start */
+            if (o.dt_floor > 0.0 && to_double(fabs(dt_new)) < o.dt_floor) { *dt_new_out = dt_new; return 2; }
             T ratio = dt_new / dt_done;
             if (fabs(ratio) < T(safety)) {
                 // rejected: re-predict from the last accepted step, or start from zero
@@ -1065,6 +1152,7 @@ struct Ias15 {
             T dtn;
             int r = step(F, h, o, st, &dtn);
             if (r < 0) { st.status = 1; return -r; }
+            if (r == 2) { st.status = 4; return 0; }
             dt = dtn;
             if (r == 1) {
                 if (last) { t = t_end; tc = 0.0; }
@@ -1179,10 +1267,10 @@ void orc_ias15_constants(double* h8, double* c49, double* d49) {
  * iterations, status.  use_dd=1 runs the double-double oracle. */
 int orc_integrate(void* h, int fbits, int gr_eih_sources, int geocentric, const double* law, double t0,
                   double t_end, int n_real, int n_var, const int* vtp, double* state, const double* params,
-                  double epsilon, double min_dt, double dt0, int max_steps, int use_dd, long long* stats,
+                  double epsilon, double min_dt, double dt0, int max_steps, double dt_floor, int use_dd, long long* stats,
                   double* t_out, double* dt_out) {
     const int N = n_real + n_var;
-    IasOpts io{epsilon, min_dt, max_steps, 12};
+    IasOpts io{epsilon, min_dt, max_steps, 12, dt_floor};
     IasStats st{0, 0, 0, 0, 0};
     int r;
     if (!use_dd) {
@@ -1221,7 +1309,7 @@ int orc_integrate_cb(orc_force_cb cb, void* ctx, double t0, double t_end, int N,
                      double epsilon, double min_dt, double dt0, int max_steps, long long* stats) {
     CallbackForces F;
     F.cb = cb; F.ctx = ctx;
-    IasOpts io{epsilon, min_dt, max_steps, 12};
+    IasOpts io{epsilon, min_dt, max_steps, 12, 0.0};
     IasStats st{0, 0, 0, 0, 0};
     Ias15<double> I(N, n_real);
     for (int i = 0; i < N; i++) for (int k = 0; k < 3; k++) { I.x0[3 * i + k] = state[6 * i + k]; I.v0[3 * i + k] = state[6 * i + 3 + k]; }
@@ -1240,7 +1328,7 @@ int orc_integrate_cb(orc_force_cb cb, void* ctx, double t0, double t_end, int N,
 int orc_integrate_batch(void* h, int fbits, int gr_eih_sources, int geocentric, const double* law, int n,
                         const double* t0, const double* t_end, double* state, const double* params,
                         int n_var_each, double* var_state, int* status, double epsilon, double min_dt,
-                        double dt0, int max_steps, int threads, long long* stats) {
+                        double dt0, int max_steps, double dt_floor, int threads, long long* stats) {
     std::atomic<int> next(0);
     std::atomic<long long> acc(0), rej(0), ev(0), it(0);
     auto work = [&]() {
@@ -1248,7 +1336,7 @@ int orc_integrate_batch(void* h, int fbits, int gr_eih_sources, int geocentric, 
         F.e = (Ephem*)h; F.o = mkopts(fbits, gr_eih_sources, geocentric, law); F.n_real = 1; F.n_var = n_var_each;
         F.vtp.assign((size_t)n_var_each, 0);
         std::vector<double> prm(3 * (size_t)(1 + n_var_each), 0.0);
-        IasOpts io{epsilon, min_dt, max_steps, 12};
+        IasOpts io{epsilon, min_dt, max_steps, 12, dt_floor};
         while (true) {
             int i = next.fetch_add(1);
             if (i >= n) break;

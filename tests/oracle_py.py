@@ -41,9 +41,9 @@ def load_lib():
                                   D, D, D]
     lib.orc_count_ops.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, D, D, C.c_int, D, D, D, L]
     lib.orc_integrate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, C.c_double, C.c_int, C.c_int, I,
-                                  D, D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, L, D, D]
+                                  D, D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, L, D, D]
     lib.orc_integrate_batch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_int, D, D, D, D, C.c_int, D, I,
-                                        C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, L]
+                                        C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, L]
     lib.orc_ias15_constants.argtypes = [D, D, D]
     return lib
 
@@ -134,7 +134,8 @@ class Oracle:
         return dict(zip(["add", "mul", "div", "sqrt", "pow"], out.tolist()))
 
     def integrate(self, t0, t_end, state, var_state=None, var_tp=None, params=None, epsilon=1e-9, min_dt=0.0,
-                  dt0=0.001, max_steps=0, dd=False, forces=0x7F, gr_eih_sources=1, geocentric=0, law=DEFAULT_LAW):
+                  dt0=0.001, max_steps=0, dd=False, forces=0x7F, gr_eih_sources=1, geocentric=0, law=DEFAULT_LAW,
+                  dt_floor=0.0):
         """One shared-step simulation (real particles then variational ones)."""
         st = np.ascontiguousarray(state, np.float64).reshape(-1, 6)
         n = st.shape[0]
@@ -158,7 +159,7 @@ class Oracle:
         law = np.asarray(law, np.float64)
         r = self.lib.orc_integrate(self.h, forces, gr_eih_sources, geocentric, _p(law), float(t0), float(t_end), n, m,
                                    None if tp is None else tp.ctypes.data_as(I), _p(buf), _p(prm), epsilon, min_dt,
-                                   dt0, max_steps, 1 if dd else 0, stats.ctypes.data_as(L), C.byref(tout),
+                                   dt0, max_steps, dt_floor, 1 if dd else 0, stats.ctypes.data_as(L), C.byref(tout),
                                    C.byref(dtout))
         out = buf.reshape(-1, 6)
         return out[:n], out[n:], dict(status=r, accepted=int(stats[0]), rejected=int(stats[1]), evals=int(stats[2]),
@@ -166,7 +167,7 @@ class Oracle:
 
     def integrate_batch(self, t0, t_end, state, params=None, var_state=None, epsilon=1e-9, min_dt=0.0, dt0=0.001,
                         max_steps=0, threads=None, forces=0x7F, gr_eih_sources=1, geocentric=0, law=DEFAULT_LAW,
-                        return_all=False):
+                        return_all=False, dt_floor=1e-8):
         st = np.ascontiguousarray(state, np.float64).reshape(-1, 6).copy()
         n = st.shape[0]
         t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,))).copy()
@@ -182,7 +183,7 @@ class Oracle:
         law = np.asarray(law, np.float64)
         self.lib.orc_integrate_batch(self.h, forces, gr_eih_sources, geocentric, _p(law), n, _p(t0), _p(te), _p(st),
                                      _p(prm), nv, _p(var), status.ctypes.data_as(I), epsilon, min_dt, dt0, max_steps,
-                                     threads or os.cpu_count() or 1, stats.ctypes.data_as(L))
+                                     dt_floor, threads or os.cpu_count() or 1, stats.ctypes.data_as(L))
         if return_all:
             return st, var, status, dict(accepted=int(stats[0]), rejected=int(stats[1]), evals=int(stats[2]),
                                          iterations=int(stats[3]))

@@ -1,6 +1,9 @@
 """Device force model against the oracle (and the reference's golden
-outputs): per-evaluation accelerations and variational accelerations within
-1e-14 relative (||a_gpu - a_ref|| <= 1e-14 ||a_ref|| per particle)."""
+outputs).  Accelerations: ||a_gpu - a_ref|| <= 1e-14 ||a_ref|| per particle.
+Variational accelerations a = J delta are measured against the scale of the
+particle's linear map: ||da_q|| <= 1e-14 max_q' ||a_q'|| over the
+variational particles of the same real particle (one delta can make J delta
+cancel to far below ||J|| ||delta||)."""
 import numpy as np
 import pytest
 
@@ -50,7 +53,10 @@ def test_forces_against_reference_golden(golden, golden_paths, dev):
         acc = np.array([[p.ax, p.ay, p.az] for p in sim.particles])
         e = rel_err(acc, ref)
         assert e[:n].max() < TOL, (hex(flags), e[:n].max())
-        assert e[n:].max() < TOL, (hex(flags), "var", e[n:].max())
+        for j in np.unique(tp):
+            q = n + np.nonzero(tp == j)[0]
+            scale = np.linalg.norm(ref[q], axis=1).max()
+            assert np.linalg.norm(acc[q] - ref[q], axis=1).max() <= TOL * scale, (hex(flags), "var", int(j))
         ex.detach(sim)
         sim.free()
 
@@ -78,7 +84,8 @@ def test_forces_each_time_vs_oracle(synth_files, dev):
             ref = O.forces(tt[i], pop.state[i:i + 1], params=pop.params[i:i + 1], var_state=var[i],
                            var_tp=np.zeros(6, np.int32), forces=flags, gr_eih_sources=gr, geocentric=geo)
             assert rel_err(acc[i], ref[0]).max() < TOL, (hex(flags), i, rel_err(acc[i], ref[0]))
-            assert rel_err(vacc[i], ref[1:]).max() < TOL, (hex(flags), i, "var")
+            scale = np.linalg.norm(ref[1:], axis=1).max()
+            assert np.linalg.norm(vacc[i] - ref[1:], axis=1).max() <= TOL * scale, (hex(flags), i, "var")
 
 
 def test_bodies_vs_oracle(synth_files, dev):

@@ -37,6 +37,7 @@
 #include "device_forces.cuh"
 #include "ias15_constants.h"
 #include "internal.h"
+#include "warp_table.cuh"
 
 #define AG_ST_OK 0
 #define AG_ST_COVERAGE 1
@@ -556,7 +557,9 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
     const DevEphem& E = *Ep;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     __shared__ AgTable tabs[4];
+    __shared__ AgWarpScratch scr[4];
     AgTable& Tab = tabs[wib];
+    AgWarpScratch& Scr = scr[wib];
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const Ws<C> W{A.ws, A.nslots, slot};
     const long long clk0 = clock64();
@@ -642,7 +645,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
             else hstep = dt;
             const bool last = live && last_group && rem == rem_min;
             /* ---- node 0: accelerations at the step start, g from the predicted b */
-            int st = ag_warp_table(E, cf, t, Tab, lane);
+            int st = ag_warp_table_fast(E, cf, t, Tab, Scr, lane);
             if (st != AG_OK) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
             if (live) {
                 double at[C];
@@ -687,7 +690,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
                 for (int n = 1; n < 8; n++) {
                     const double hn = ag_ias.h[n];
                     const double tn = t + (tc + hstep * hn);
-                    st = ag_warp_table(E, cf, tn, Tab, lane);
+                    st = ag_warp_table_fast(E, cf, tn, Tab, Scr, lane);
                     if (st != AG_OK) break;
                     if (!conv) {
                         double sx[9], sv[8];

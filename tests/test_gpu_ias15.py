@@ -28,8 +28,12 @@ def test_batch_vs_oracle_mixture(synth_files, group_steps):
     o = batch.options(group_steps=group_steps)
     out, _, status, stats = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params, opts=o)
     ref, _, rstat, rstats = O.integrate_batch(pop.t0, pop.t_end, pop.state, params=pop.params, return_all=True)
-    assert (status == 0).all() and (rstat == 0).all()
-    dx = np.abs(out[:, :3] - ref[:, :3]).max(axis=1)
+    # the 1 % close-approach class holds a few Earth impactors: both sides
+    # stop them with the step-underflow status, the rest complete
+    assert np.array_equal(status, rstat), (np.nonzero(status)[0], np.nonzero(rstat)[0])
+    assert set(np.unique(rstat)) <= {0, 4} and (rstat == 0).mean() > 0.98
+    ok = rstat == 0
+    dx = np.abs(out[ok, :3] - ref[ok, :3]).max(axis=1)
     assert dx.max() < 1e-9, dx.max()
     if group_steps == 0:
         assert np.median(dx) < 1e-12

@@ -63,6 +63,10 @@ clib.assist_gb300_integrate_batch.restype = c_int
 clib.assist_gb300_integrate_batch_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p,
                                                      c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
 clib.assist_gb300_integrate_batch_device.restype = c_int
+clib.assist_gb300_integrate_batch_device_static.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p,
+                                                            c_void_p, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
+clib.assist_gb300_integrate_batch_device_static.restype = c_int
+STATIC_MAX_PARTICLES = 1048576       # ASSIST_GB300_STATIC_MAX_PARTICLES
 clib.assist_gb300_forces_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p, c_int,
                                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_forces_device.restype = c_int

@@ -77,6 +77,23 @@ def integrate_batch_device(ephem: Ephem, t0, t_end, state, params=None, var_stat
     return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
 
 
+def integrate_batch_device_static(ephem: Ephem, t0, t_end, state, params=None, status=None,
+                                  opts: Optional[Options] = None, stream=None):
+    """integrate_batch_device with independent steps and no variational
+    particles, through the entry point that allocates nothing (its scratch is
+    a fixed device array; at most STATIC_MAX_PARTICLES particles; one call at a
+    time per device)."""
+    o = opts or options()
+    n = state.shape[0]
+    stats = BatchStats()
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_integrate_batch_device_static(byref(ephem), byref(o), n, _ptr(t0), _ptr(t_end), _ptr(state),
+                                                         _ptr(params), _ptr(status), s, byref(stats))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_integrate_batch_device_static failed (%d): %s" % (rc, last_error()))
+    return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
+
+
 def forces_device(ephem: Ephem, t, state, params=None, var_state=None, acc=None, var_acc=None, status=None,
                   opts: Optional[Options] = None, stream=None):
     """One force evaluation of n particles at their own times t[i] (torch CUDA tensors)."""

@@ -73,6 +73,12 @@ static ForceCfg make_cfg(int forces, int gr, int geo, double alpha, double nk, d
     c.s_ca = std::cos(ras); c.s_sa = std::sin(ras); c.s_cd = std::cos(decs); c.s_sd = std::sin(decs);
     return c;
 }
+
+/* The force configuration of a set of batch options (used by the other
+ * translation units' entry points). */
+ForceCfg ag_make_cfg(const struct assist_gb300_options* o) {
+    return make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
+}
 static ForceCfg cfg_of(const struct assist_extras* ax) {
     return make_cfg(ax->forces, ax->gr_eih_sources, ax->geocentric, ax->alpha, ax->nk, ax->nm, ax->nn, ax->r0);
 }

@@ -354,6 +354,10 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     return ASSIST_SUCCESS;
 }
 
+int ag_ephem_view_ready(const struct assist_ephem* e) {
+    return e && e->ascii_planets && e->ascii_planets->d_view ? 1 : 0;
+}
+
 double ag_sun_gm(const struct assist_ephem* e) { return e->ascii_planets->mass[ASSIST_BODY_SUN]; }
 
 int ag_ephem_n_bodies(const struct assist_ephem* e) {

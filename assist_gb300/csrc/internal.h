@@ -67,6 +67,16 @@ struct AgSharedSim;
 AgSharedSim* ag_shared_create(void);
 void ag_shared_free(AgSharedSim* s);
 
+struct assist_gb300_options;
+ForceCfg ag_make_cfg(const struct assist_gb300_options* o);
+
+struct assist_ephem;
+/* The device view of an ephemeris (uploaded on first use). */
+int ag_ephem_device(const struct assist_ephem* e, DevEphem* out);
+
+/* 1 when the ephemeris's device view exists (ag_ephem_device will not allocate) */
+int ag_ephem_view_ready(const struct assist_ephem* e);
+
 /* library error state */
 void ag_set_error(const std::string& msg);
 int ag_cuda_check(cudaError_t e, const char* what);

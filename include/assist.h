@@ -260,6 +260,29 @@ int assist_gb300_integrate_batch_device(const struct assist_ephem* ephem, const 
                                         int* d_status, void* stream,
                                         struct assist_gb300_batch_stats* stats);
 
+/* Batched IAS15 that allocates nothing (no counterpart in the reference).
+ * Same integration as assist_gb300_integrate_batch_device with
+ * group_steps = 0 and n_var = 0 (independent per-particle steps, identical
+ * end states), for callers that cannot allocate device memory at call time:
+ * a process whose free device memory is already claimed by another
+ * allocator, or a loop that must not take the implicit device-wide
+ * synchronisation of cudaFree.  Its scratch (queue, counters, workspace) is
+ * one fixed __device__ array of ASSIST_GB300_STATIC_SCRATCH_BYTES per device;
+ * n above ASSIST_GB300_STATIC_MAX_PARTICLES is rejected with
+ * ASSIST_ERROR_N.  The ephemeris must already have a device view (one
+ * ordinary device call with it first).  The first call on a device looks up
+ * the scratch address and uploads the IAS15 tables: make it before any stream
+ * capture.  One scratch per device: calls that overlap in time on one device
+ * (other streams or threads) race on it and must be serialised by the caller.
+ * stats->kernel_ms is -1 (not timed). */
+#define ASSIST_GB300_STATIC_SCRATCH_BYTES (32 << 20)
+#define ASSIST_GB300_STATIC_MAX_PARTICLES 1048576
+int assist_gb300_integrate_batch_device_static(const struct assist_ephem* ephem,
+                                               const struct assist_gb300_options* opt, int n,
+                                               const double* d_t0, const double* d_t_end, double* d_state,
+                                               const double* d_params, int* d_status, void* stream,
+                                               struct assist_gb300_batch_stats* stats);
+
 /* One force evaluation for n particles at per-particle times t[i] (device
  * pointers): acc[3i..3i+2] = a(x_i, v_i, t_i) for the force model in `opt`.
  * With n_var = 6, var_state holds per-particle 6 variational states (6 doubles

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_int, c_longlong, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_longlong, c_ulonglong, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.environ.get("ASSIST_GB300_LIB", os.path.join(HERE, "libassist_gb300.so"))
@@ -67,6 +67,25 @@ clib.assist_gb300_integrate_batch_device_static.argtypes = [c_void_p, POINTER(Op
                                                             c_void_p, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
 clib.assist_gb300_integrate_batch_device_static.restype = c_int
 STATIC_MAX_PARTICLES = 1048576       # ASSIST_GB300_STATIC_MAX_PARTICLES
+clib.assist_gb300_warm_n_params.restype = c_int
+clib.assist_gb300_warm_init.argtypes = [c_ulonglong]
+clib.assist_gb300_warm_init.restype = c_int
+clib.assist_gb300_warm_set_params.argtypes = [c_void_p, c_int]
+clib.assist_gb300_warm_set_params.restype = c_int
+clib.assist_gb300_warm_get_params.argtypes = [c_void_p, c_int]
+clib.assist_gb300_warm_get_params.restype = c_int
+clib.assist_gb300_warm_grad.argtypes = [c_void_p, c_void_p, c_int, c_void_p, POINTER(c_double)]
+clib.assist_gb300_warm_grad.restype = c_int
+clib.assist_gb300_warm_adam_step.argtypes = [c_void_p, c_float]
+clib.assist_gb300_warm_adam_step.restype = c_int
+clib.assist_gb300_warm_train.argtypes = [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_ulonglong,
+                                         POINTER(c_double)]
+clib.assist_gb300_warm_train.restype = c_int
+clib.assist_gb300_warm_infer.argtypes = [c_void_p, c_int, c_void_p]
+clib.assist_gb300_warm_infer.restype = c_int
+clib.assist_gb300_warm_set_log.argtypes = [c_void_p, c_void_p, c_int, c_int]
+clib.assist_gb300_warm_set_log.restype = c_int
+clib.assist_gb300_warm_log_count.restype = c_int
 clib.assist_gb300_forces_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p, c_int,
                                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_forces_device.restype = c_int

@@ -540,7 +540,7 @@ extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
     o->max_steps = 1000000;
     o->warm_start = 0;
     o->threads_per_block = 0;
-    o->group_steps = 1;
+    o->group_steps = 2;
     o->dt_floor = 1e-8;
 }
 
@@ -592,6 +592,14 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
     if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
     if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
+    if (o->warm_start && (o->group_steps != 2 || n_var != 0)) {
+        ag_set_error("the learned warm start runs in the block-cooperative kernel: group_steps = 2, n_var = 0");
+        return ASSIST_ERROR_N;
+    }
+    if (o->warm_start && !ag_mlp_device_view()) {
+        ag_set_error("warm_start = 1 needs a network (assist_gb300_warm_init, _set_params or _train first)");
+        return ASSIST_ERROR_N;
+    }
     DevEphem D;
     int st = ag_ephem_device(e, &D);
     if (st) return st;
@@ -686,7 +694,13 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
         gsize.swap(z2);
     }
     int nslots;
-    if (grouped) {
+    const bool coop = o->group_steps == 2;
+    if (coop) {
+        /* one 32-particle group per 128-thread block */
+        nslots = ag_coop_max_slots(n_var);
+        const int need = 32 * (int)gstart.size();
+        if (nslots > need) nslots = need;
+    } else if (grouped) {
         nslots = ag_group_max_slots(n_var);
         const int need = 32 * (int)gstart.size();
         if (nslots > need) nslots = ((need + 127) / 128) * 128;
@@ -735,6 +749,14 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
     a.dt_floor = o->dt_floor;
     if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
+    if (coop && n_var == 0) {
+        if (o->warm_start) a.mlp = ag_mlp_device_view();
+        float *lx = nullptr, *lt = nullptr;
+        int cap = 0, every = 1, *cnt = nullptr;
+        if (ag_mlp_log_config(&lx, &lt, &cap, &every, &cnt)) {
+            a.log_x = lx; a.log_t = lt; a.log_cap = cap; a.log_every = every; a.log_count = cnt;
+        }
+    }
     /* per-thread run-time budget: ASSIST_GB300_WATCHDOG_S seconds (default 300) at the boost clock */
     double wd = 300.0;
     if (const char* w = getenv("ASSIST_GB300_WATCHDOG_S")) wd = atof(w);
@@ -742,7 +764,8 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int le = grouped ? ag_launch_group(D, c, a, n_var, s) : ag_launch_batch(D, c, a, n_var, tpb, s);
+    int le = coop ? ag_launch_coop(D, c, a, n_var, s)
+                  : (grouped ? ag_launch_group(D, c, a, n_var, s) : ag_launch_batch(D, c, a, n_var, tpb, s));
     cudaEventRecord(e1, s);
     if (le) { cudaEventDestroy(e0); cudaEventDestroy(e1); ag_cuda_check((cudaError_t)le, "batch kernel launch"); return ASSIST_ERROR_EPHEM_FILE; }
     if (stats) {

@@ -1,0 +1,786 @@
+/*
+ * ias15_coop.cuh -- block-cooperative grouped batched IAS15 (included by
+ * kernels_ias15.cu, after the warp-grouped kernel whose helpers it uses).
+ *
+ * A group of up to 32 particles that share their step times (the same
+ * grouping as the warp-grouped kernel) is integrated by one 128-thread block:
+ * lane l of every warp works on particle l, and the four warps split the
+ * work of each force evaluation so that it runs on all four SM sub-partitions
+ * (each has its own FP64 pipe):
+ *
+ *   warp 0  planets' direct gravity (ASSIST's order, Sun last), Marsden
+ *           non-gravitational term, geocentric indirect term
+ *   warp 1  EIH/PPN relativity (its per-source sums too), GR potential/simple
+ *   warp 2  first half of the asteroids, Earth J2-J4
+ *   warp 3  second half of the asteroids, Sun J2
+ *
+ * The partial accelerations (and partial Jacobians) meet in shared memory and
+ * are summed in a fixed order ((w3 + w2) + w1) + w0, so the planets' terms,
+ * the largest, come last as in ASSIST's sum.  The body table of each
+ * substep time is built by the whole block: column components of the .440
+ * record and asteroid components of the SPK records on different threads, in
+ * the reference's exact arithmetic.  Each IAS15 state component has an owner
+ * warp that predicts it, forms its acceleration from the partials and
+ * updates its g, b and e: x, y, z belong to warps 1, 2, 3; the three
+ * components of a variational particle share one warp (its J.dx product reads
+ * only its own predicted values).
+ * Per-particle control values (t, dt, convergence, retirement) are computed
+ * identically by all four warps from shared data, so every branch around a
+ * block barrier is uniform.
+ *
+ * Per evaluation this cuts the FP64 instructions on one sub-partition to
+ * roughly a third of the warp-grouped kernel's, which is what bounds the
+ * longest groups (the tail of a batch).
+ */
+
+/* Raw sums of one substep time, shared by the block. */
+struct AgCoopScratch {
+    double col[11][3];              /* .440 column position sums (km) */
+    double sun_v[3];                /* Sun velocity sums (km/s) */
+    double ast_h[AG_MAX_AST][3];    /* heliocentric asteroid positions (AU) */
+};
+
+/* Table pass 1: column and asteroid component sums.  Returns this thread's
+ * coverage status (combined by the caller's barrier). */
+__device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const ForceCfg& c, double t, AgCoopScratch& S,
+                                                   int tid) {
+    int bad = 0;
+    if (tid < 64) {
+        const int lane = tid & 31;
+        const bool w0 = tid < 32;
+        if ((w0 && lane < 30) || (!w0 && lane < 3)) {
+            const double* rec = nullptr;
+            double tf = 0.0;
+            if (ag_planet_record(E, t, &rec, &tf) != AG_OK) {
+                bad = 1;
+            } else if (w0) {
+                /* MER..LUN (columns 0..9), component lane % 3 */
+                S.col[lane / 3][lane % 3] = ag_colcomp_exact<false>(E, rec, lane / 3, lane % 3, tf, nullptr);
+            } else {
+                double vs;
+                S.col[AG_C_SUN][lane] = ag_colcomp_exact<true>(E, rec, AG_C_SUN, lane, tf, &vs);
+                S.sun_v[lane] = vs;
+            }
+        }
+    } else {
+        const bool need = (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) != 0;
+        for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
+            double h = 0.0;
+            if (ag_astcomp_exact(E, task / 3, task % 3, t, &h) != AG_OK && need) bad = 1;
+            S.ast_h[task / 3][task % 3] = h;
+        }
+    }
+    return bad;
+}
+
+/* Table pass 2: bodies in AU (Earth and Moon from the Earth-Moon barycentre),
+ * the Sun's velocity, barycentric asteroids, further EIH velocities and the
+ * geocentric Earth acceleration. */
+__device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const ForceCfg& c, double t, AgTable& T,
+                                                    const AgCoopScratch& S, int tid) {
+    if (tid < 33) {
+        const int b = tid / 3, comp = tid % 3;
+        double u;
+        if (b == AG_EAR) u = __dadd_rn(S.col[AG_C_EMB][comp], __dmul_rn(S.col[AG_C_LUN][comp], E.f_earth));
+        else if (b == AG_MOO) u = __dadd_rn(S.col[AG_C_EMB][comp], __dmul_rn(S.col[AG_C_LUN][comp], E.f_moon));
+        else u = S.col[ag_col_of(b)][comp];
+        const double x = __ddiv_rn(u, E.pl_cau);
+        if (comp == 0) T.P.x[b] = x; else if (comp == 1) T.P.y[b] = x; else T.P.z[b] = x;
+    } else if (tid < 36) {
+        const int comp = tid - 33;
+        const double v = __ddiv_rn(S.sun_v[comp], E.cau_per_day);
+        if (comp == 0) T.P.vx[AG_SUN] = v; else if (comp == 1) T.P.vy[AG_SUN] = v; else T.P.vz[AG_SUN] = v;
+    } else if (tid >= 64) {
+        for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
+            const int comp = task % 3;
+            const double sun = __ddiv_rn(S.col[AG_C_SUN][comp], E.pl_cau);
+            T.ast[task / 3][comp] = __dadd_rn(S.ast_h[task / 3][comp], sun);
+        }
+        int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
+        if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
+        const int j = tid - 96;                 /* warp 3: one lane per further source */
+        if (nv > 1 && j > 0 && j < nv && j < AG_NPL) {
+            const double* rec = nullptr;
+            double tf = 0.0;
+            if (ag_planet_record(E, t, &rec, &tf) == AG_OK) ag_table_velocity(E, rec, tf, j, T);
+        }
+        if (c.geocentric == 1 && tid == 127) ag_table_earth_acc(E, t, T);
+    }
+}
+
+/* EIH per-source sums (Newtonian acceleration of source j by the other
+ * planets, sum GM_k / r_jk), one lane per other planet, by one warp. */
+__device__ __forceinline__ void ag_coop_eih_sources(const DevEphem& E, const ForceCfg& c, AgTable& T, int lane) {
+    for (int j = 0; j < c.gr_eih_sources && j < AG_NPL; j++) {
+        double ax = 0.0, ay = 0.0, az = 0.0, s1 = 0.0;
+        if (lane < AG_NPL && lane != j) {
+            const int k = lane;
+            const double dx = T.P.x[j] - T.P.x[k], dy = T.P.y[j] - T.P.y[k], dz = T.P.z[j] - T.P.z[k];
+            const double ri = rsqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+            const double gri = E.gm[k] * ri;
+            s1 = gri;
+            const double f = gri * ri * ri;
+            ax = -f * dx; ay = -f * dy; az = -f * dz;
+        }
+        for (int o = 8; o > 0; o >>= 1) {
+            ax += __shfl_down_sync(AG_FULL, ax, o, 16);
+            ay += __shfl_down_sync(AG_FULL, ay, o, 16);
+            az += __shfl_down_sync(AG_FULL, az, o, 16);
+            s1 += __shfl_down_sync(AG_FULL, s1, o, 16);
+        }
+        if (lane == 0) { T.eih_a[j][0] = ax; T.eih_a[j][1] = ay; T.eih_a[j][2] = az; T.eih_t1[j] = s1; }
+    }
+    __syncwarp();
+}
+
+/* Warp w's share of the force evaluation at (x, v): partial acceleration and,
+ * with JAC, partial 3x6 Jacobian. */
+template <bool JAC>
+__device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const DevEphem& E, const ForceCfg& c,
+                                                  const double* x, const double* v, const double* A, double* acc,
+                                                  double (*J)[6]) {
+    const TableBodies B(T);
+    const PlanetState& P = T.P;
+    double xo[3], vo[3], ao[3];
+    ag_origin(c, P, xo, vo, ao);
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (JAC)
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 6; b++) J[a][b] = 0.0;
+    const bool direct = (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) != 0;
+    int st = AG_OK;
+    if (w == 0) {
+        double dx[AG_NPL], dy[AG_NPL], dz[AG_NPL], ri[AG_NPL];
+#pragma unroll
+        for (int k = 0; k < AG_NPL; k++) ag_sep(P, x, xo, k, dx[k], dy[k], dz[k], ri[k]);
+        if ((c.forces & AG_F_NONGRAV) && A != nullptr && (A[0] != 0.0 || A[1] != 0.0 || A[2] != 0.0)) {
+            const double d[3] = {dx[AG_SUN], dy[AG_SUN], dz[AG_SUN]};
+            const double dv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
+            double JA[3][3];
+            bool has_ng;
+            ag_term_nongrav<JAC>(c, d, ri[AG_SUN], dv, A, ax, ay, az, J, JA, &has_ng);
+        }
+        if (direct) {
+#pragma unroll
+            for (int q = 0; q < AG_NPL; q++) {
+                const int k = ag_planet_order(q);
+                const bool on = (k == AG_SUN) ? (c.forces & AG_F_SUN) : (c.forces & AG_F_PLANETS);
+                ag_term_planet<JAC>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, J);
+            }
+        }
+        if (c.geocentric == 1) { ax -= ao[0]; ay -= ao[1]; az -= ao[2]; }
+    } else if (w == 1) {
+        if (c.forces & AG_F_EIH) {
+            double dx[AG_NPL], dy[AG_NPL], dz[AG_NPL], ri[AG_NPL];
+#pragma unroll
+            for (int k = 0; k < AG_NPL; k++) ag_sep(P, x, xo, k, dx[k], dy[k], dz[k], ri[k]);
+            ag_term_eih<TableBodies, JAC>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, J);
+        }
+        if (c.forces & (AG_F_GR_POT | AG_F_GR_SIMPLE)) {
+            double p[3], ri;
+            ag_sep(P, x, xo, AG_SUN, p[0], p[1], p[2], ri);
+            if (c.forces & AG_F_GR_POT) ag_term_gr_pot<JAC>(E, p, ri, ax, ay, az, J);
+            if (c.forces & AG_F_GR_SIMPLE) {
+                const double pv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
+                ag_term_gr_simple<JAC>(E, p, ri, pv, ax, ay, az, J);
+            }
+        }
+    } else {
+        const bool on_ast = (c.forces & AG_F_AST) != 0;
+        const int h = (E.n_ast + 1) / 2;
+        if (direct && (on_ast || JAC))
+            st = ag_term_asteroids<TableBodies, JAC>(B, E, on_ast, x, xo, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay,
+                                                     az, J);
+        if (w == 2 && (c.forces & AG_F_EARTH_H)) {
+            double dx, dy, dz, ri;
+            ag_sep(P, x, xo, AG_EAR, dx, dy, dz, ri);
+            ag_term_earth_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
+        }
+        if (w == 3 && (c.forces & AG_F_SUN_H)) {
+            double dx, dy, dz, ri;
+            ag_sep(P, x, xo, AG_SUN, dx, dy, dz, ri);
+            ag_term_sun_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
+        }
+    }
+    acc[0] = ax; acc[1] = ay; acc[2] = az;
+    return st;
+}
+
+/* b, e of one component from the last accepted step's br, er (the shift of
+ * the acceleration polynomial to the new step). */
+template <int C>
+__device__ __forceinline__ void ag_predict_next_comp(const Ws<C>& W, int comp, double ratio) {
+    if (ratio > 20.0) {
+        for (int k = 0; k < 7; k++) { W(W_E + k, comp) = 0.0; W(W_B + k, comp) = 0.0; }
+        return;
+    }
+    double q[8];
+    q[1] = ratio;
+    for (int k = 2; k < 8; k++) q[k] = q[k - 1] * ratio;
+    constexpr double binom[8][8] = {
+        {1, 0, 0, 0, 0, 0, 0, 0}, {1, 1, 0, 0, 0, 0, 0, 0}, {1, 2, 1, 0, 0, 0, 0, 0}, {1, 3, 3, 1, 0, 0, 0, 0},
+        {1, 4, 6, 4, 1, 0, 0, 0}, {1, 5, 10, 10, 5, 1, 0, 0}, {1, 6, 15, 20, 15, 6, 1, 0}, {1, 7, 21, 35, 35, 21, 7, 1}};
+    double br[7], er[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++) { br[k] = W(W_BR + k, comp); er[k] = W(W_ER + k, comp); }
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 6; k >= j; k--) s = fma(br[k], binom[k + 1][j + 1], s);
+        const double e = q[j + 1] * s;
+        W(W_E + j, comp) = e;
+        W(W_B + j, comp) = e + (br[j] - er[j]);
+    }
+}
+
+/* Owner warp of IAS15 component comp: x, y, z -> warps 1..3; variational
+ * particles 0..5 -> warps 0, 0, 1, 2, 3, 1. */
+__device__ __forceinline__ int ag_coop_owner(int comp) {
+    if (comp < 3) return comp + 1;
+    const int q = (comp - 3) / 3;
+    return q < 2 ? 0 : ((q == 2 || q == 5) ? 1 : (q == 3 ? 2 : 3));
+}
+
+template <int NV>
+struct AgCoopShared {
+    static constexpr int C = 3 * (1 + NV);
+    AgTable tab;
+    AgCoopScratch scr;
+    double xs[C][32], vs[C][32];                    /* state at the current node */
+    double pa[4][3][32];                            /* partial accelerations */
+    double pj[NV > 0 ? 4 : 1][NV > 0 ? 18 : 1][32]; /* partial Jacobians */
+    double ra[3][32], rdb[3][32];                   /* |a|, |delta b6| of x, y, z at node 7 */
+    double rb6[3][32];                              /* |b6| of x, y, z after convergence */
+    int fin[3][32];
+    int g, stop;
+};
+
+/* Shared buffers of the learned warm start (dynamic shared memory, present
+ * only when a network is loaded or steps are logged). */
+struct AgWarmSmem {
+    AgMlpSmem M;
+    double corr[7][3][32];          /* (br - er)_kc of each lane */
+    float bpa[7][3][32];            /* |b_pred_kc| */
+    float tgt[7][3][32];            /* logged targets */
+    float xf[32][AG_MLP_IN + 1];    /* features of this step (logged with the target) */
+    double kappa[7][32];
+    int valid[32];
+};
+
+/* Distance from (x, y, z) to the nearest of the eleven planets in the table. */
+__device__ __forceinline__ double ag_nearest_planet(const AgTable& T, double x, double y, double z) {
+    double m = 1e300;
+#pragma unroll
+    for (int k = 0; k < AG_NPL; k++) {
+        const double dx = x - T.P.x[k], dy = y - T.P.y[k], dz = z - T.P.z[k];
+        m = fmin(m, fma(dx, dx, fma(dy, dy, dz * dz)));
+    }
+    return sqrt(m);
+}
+
+template <int NV, bool WARM>
+__global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
+    constexpr int C = 3 * (1 + NV);
+    const DevEphem& E = *Ep;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    __shared__ AgCoopShared<NV> S;
+    AgTable& Tab = S.tab;
+    const int slot = blockIdx.x * 32 + lane;
+    const Ws<C> W{A.ws, A.nslots, slot};
+    const long long clk0 = clock64();
+    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
+    if (tid == 0) { Tab.status = AG_OK; S.stop = 0; }
+    /* learned warm start and step logging (no variational particles) */
+    extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
+    AgWarmSmem& WS = *reinterpret_cast<AgWarmSmem*>(ag_dyn_smem);
+    const bool warm = WARM && NV == 0 && A.mlp != nullptr;
+    const bool logp = WARM && NV == 0 && A.log_x != nullptr;
+
+    while (true) {
+        __syncthreads();
+        if (tid == 0) S.g = S.stop ? A.n_groups : atomicAdd(A.queue, 1);
+        __syncthreads();
+        const int g = S.g;
+        if (g >= A.n_groups) break;
+        const int gs = A.grp_size[g], g0 = A.grp_start[g];
+        const int pid = lane < gs ? A.order[g0 + lane] : -1;
+        double t = A.t0[A.order[g0]], tc = 0.0, dtls = 0.0;
+        const double tend = pid >= 0 ? A.t_end[pid] : t;
+        double dir;
+        {
+            const double d = pid >= 0 ? (tend - t) : 0.0;
+            const unsigned fwd = __ballot_sync(AG_FULL, d > 0.0), bwd = __ballot_sync(AG_FULL, d < 0.0);
+            dir = fwd ? 1.0 : (bwd ? -1.0 : 1.0);
+        }
+        double dt = dir * fabs(A.dt0);
+        double prm[3] = {0.0, 0.0, 0.0};
+        bool has_prm = false;
+        int pstat = AG_ST_OK;
+        bool live = pid >= 0;
+        if (live) {
+            const double* s0 = A.state + 6 * (size_t)pid;
+            for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                double x0, v0;
+                if (comp < 3) { x0 = s0[comp]; v0 = s0[3 + comp]; }
+                else {
+                    const double* vs = A.var_state + ((size_t)pid * NV + (comp - 3) / 3) * 6;
+                    x0 = vs[(comp - 3) % 3]; v0 = vs[3 + (comp - 3) % 3];
+                }
+                W(W_X0, comp) = x0; W(W_V0, comp) = v0; W(W_XC, comp) = 0.0; W(W_VC, comp) = 0.0;
+                for (int k = 0; k < 7; k++) {
+                    W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; W(W_BR + k, comp) = 0.0; W(W_ER + k, comp) = 0.0;
+                }
+            }
+            if (A.params) {
+                prm[0] = A.params[3 * (size_t)pid]; prm[1] = A.params[3 * (size_t)pid + 1]; prm[2] = A.params[3 * (size_t)pid + 2];
+                has_prm = true;
+            }
+        }
+        bool finish_now = live && (tend == t);
+        long long steps = 0;
+        /* warm start per lane: on until its learned starts converge slower than
+         * the plain predictor's (every 8th step is a plain probe) */
+        bool wl_on = warm;
+        int wl_sum_l = 0, wl_n_l = 0, wl_sum_p = 0, wl_n_p = 0;
+        while (true) {
+            /* ---- retire lanes whose particle is complete */
+            if (__any_sync(AG_FULL, finish_now)) {
+                if (finish_now) {
+                    for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                        const double x1 = W(W_X0, comp) + W(W_XC, comp), v1 = W(W_V0, comp) + W(W_VC, comp);
+                        if (comp < 3) {
+                            double* s0 = A.state + 6 * (size_t)pid;
+                            s0[comp] = x1; s0[3 + comp] = v1;
+                            S.fin[comp][lane] = isfinite(x1) && isfinite(v1);
+                        } else {
+                            double* vs = A.var_state + ((size_t)pid * NV + (comp - 3) / 3) * 6;
+                            vs[(comp - 3) % 3] = x1; vs[3 + (comp - 3) % 3] = v1;
+                        }
+                    }
+                }
+                __syncthreads();
+                if (finish_now) {
+                    const bool finite = S.fin[0][lane] && S.fin[1][lane] && S.fin[2][lane];
+                    if (pstat == AG_ST_OK && !finite) pstat = AG_ST_NONFINITE;
+                    if (wid == 0 && A.status) A.status[pid] = pstat;
+                    live = false;
+                    finish_now = false;
+                }
+            }
+            if (!__any_sync(AG_FULL, live)) break;
+            /* ---- watchdog (thread 0 decides for the block) */
+            if (tid == 0 && A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles) S.stop = 1;
+            __syncthreads();
+            if (S.stop) {
+                pstat = AG_ST_TIMEOUT;
+                finish_now = live;
+                continue;
+            }
+            /* ---- step size: no further than the nearest unfinished end */
+            const double rem = live ? fabs((tend - t) - tc) : 1e300;
+            const double rem_min = warp_min(rem);
+            double hstep;
+            bool last_group = false;
+            if (fabs(dt) >= rem_min) { hstep = dir * rem_min; last_group = true; }
+            else hstep = dt;
+            const bool last = live && last_group && rem == rem_min;
+
+            /* ---- node 0: accelerations at the step start, g from the predicted b */
+            int bad = ag_coop_table_pass1(E, cf, t, S.scr, tid);
+            if (live)
+                for (int comp = 0; comp < C; comp++)
+                    if (ag_coop_owner(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
+            bad = __syncthreads_or(bad);
+            if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            ag_coop_table_pass2(E, cf, t, Tab, S.scr, tid);
+            __syncthreads();
+            if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
+            int fst = AG_OK;
+            if (live) {
+                const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
+                const double vp[3] = {S.vs[0][lane], S.vs[1][lane], S.vs[2][lane]};
+                double acc[3];
+                if (NV > 0) {
+                    double J[3][6];
+                    fst = ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
+                } else {
+                    fst = ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                }
+                S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
+                if (wid == 0) n_ev++;
+            }
+            bad = __syncthreads_or(fst != AG_OK);
+            if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            if (live) {
+                for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                    double at;
+                    if (comp < 3) {
+                        at = ((S.pa[3][comp][lane] + S.pa[2][comp][lane]) + S.pa[1][comp][lane]) + S.pa[0][comp][lane];
+                    } else {
+                        const int q = (comp - 3) / 3, a = (comp - 3) % 3;
+                        double Jr[6];
+                        for (int b = 0; b < 6; b++)
+                            Jr[b] = ((S.pj[3][6 * a + b][lane] + S.pj[2][6 * a + b][lane]) + S.pj[1][6 * a + b][lane]) +
+                                    S.pj[0][6 * a + b][lane];
+                        const double* dxq = &S.xs[3 + 3 * q][0];
+                        const double* dvq = &S.vs[3 + 3 * q][0];
+                        double s = Jr[0] * dxq[lane];
+                        s = fma(Jr[1], dxq[32 + lane], s); s = fma(Jr[2], dxq[64 + lane], s);
+                        s = fma(Jr[3], dvq[lane], s); s = fma(Jr[4], dvq[32 + lane], s); s = fma(Jr[5], dvq[64 + lane], s);
+                        at = s;
+                    }
+                    W(W_A0, comp) = at;
+                }
+            }
+            /* ---- learned warm start: features, BF16 inference, b += kappa y */
+            bool w_applied = false, w_probe = false;
+            if (warm || logp) {
+                if (live && wid >= 1)
+                    for (int k = 0; k < 7; k++) {
+                        WS.corr[k][wid - 1][lane] = W(W_BR + k, wid - 1) - W(W_ER + k, wid - 1);
+                        WS.bpa[k][wid - 1][lane] = (float)fabs(W(W_B + k, wid - 1));
+                    }
+                __syncthreads();
+                if (wid == 0) {
+                    bool ok = false;
+                    if (live) {
+                        double corr[7][3], kap[7];
+                        float bpa[7][3], x[AG_MLP_IN];
+                        for (int k = 0; k < 7; k++)
+                            for (int c = 0; c < 3; c++) { corr[k][c] = WS.corr[k][c][lane]; bpa[k][c] = WS.bpa[k][c][lane]; }
+                        const double x0 = W(W_X0, 0), y0 = W(W_X0, 1), z0 = W(W_X0, 2);
+                        const double rx = sqrt(fma(x0, x0, fma(y0, y0, z0 * z0)));
+                        ok = ag_warm_features(corr, bpa, hstep, dtls, rx, ag_nearest_planet(Tab, x0, y0, z0), x, kap);
+                        for (int k = 0; k < 7; k++) WS.kappa[k][lane] = kap[k];
+                        for (int i = 0; i < AG_MLP_IN; i++) { WS.xf[lane][i] = x[i]; WS.M.X[lane][i] = __float2bfloat16_rn(x[i]); }
+                    } else {
+                        for (int i = 0; i < AG_MLP_IN; i++) WS.M.X[lane][i] = __float2bfloat16_rn(0.0f);
+                    }
+                    WS.valid[lane] = ok ? 1 : 0;
+                }
+                __syncthreads();
+                const bool valid = live && WS.valid[lane];
+                w_probe = valid && wl_on && (steps & 7) == 7;
+                const bool want = valid && wl_on && !w_probe;
+                if (__syncthreads_or(want)) {
+                    ag_mlp_infer_block(*A.mlp, WS.M, wid, lane);
+                    if (want) {
+                        bool ok_y = true;
+                        for (int o = 0; o < AG_MLP_OUT; o++) {
+                            const float y = WS.M.Y[lane][o];
+                            ok_y = ok_y && isfinite(y) && fabsf(y) <= AG_MLP_YCLIP;
+                        }
+                        if (ok_y) {
+                            w_applied = true;
+                            if (wid >= 1)
+                                for (int k = 0; k < 7; k++)
+                                    W(W_B + k, wid - 1) = fma(WS.kappa[k][lane], (double)WS.M.Y[lane][3 * k + wid - 1],
+                                                              W(W_B + k, wid - 1));
+                            if (wid == 0) n_wused++;
+                        } else if (wid == 0) {
+                            n_wfall++;
+                        }
+                    }
+                }
+            }
+            if (live) {
+                for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                    double b[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+#pragma unroll
+                    for (int j = 0; j < 7; j++) {
+                        double s = b[j];
+#pragma unroll
+                        for (int k = j + 1; k < 7; k++) s = fma(b[k], ag_ias.d[j][k], s);
+                        W(W_G + j, comp) = s;
+                    }
+                }
+            }
+            /* ---- predictor-corrector iterations */
+            int iters = 1, it_lane = 0;
+            double pc_last = 1e300, ma7 = 0.0;
+            bool conv = !live;
+            bool cov = false;
+            while (true) {
+                for (int n = 1; n < 8; n++) {
+                    const double hn = ag_ias.h[n];
+                    const double tn = t + (tc + hstep * hn);
+                    bad = ag_coop_table_pass1(E, cf, tn, S.scr, tid);
+                    if (!conv) {
+                        double sx[9], sv[8];
+                        sx[0] = hstep * hn;
+                        sx[1] = sx[0] * sx[0] * 0.5;
+#pragma unroll
+                        for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * ag_ias.fx[n][k];
+                        sv[0] = hstep * hn;
+#pragma unroll
+                        for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * ag_ias.fv[n][k];
+                        for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                            double px = sx[8] * W(W_B + 6, comp);
+#pragma unroll
+                            for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, comp), px);
+                            px = fma(sx[1], W(W_A0, comp), px);
+                            px = fma(sx[0], W(W_V0, comp), px);
+                            S.xs[comp][lane] = W(W_X0, comp) + (px + W(W_XC, comp));
+                            double pv = sv[7] * W(W_B + 6, comp);
+#pragma unroll
+                            for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(W_B + j, comp), pv);
+                            pv = fma(sv[0], W(W_A0, comp), pv);
+                            S.vs[comp][lane] = W(W_V0, comp) + (pv + W(W_VC, comp));
+                        }
+                    }
+                    bad = __syncthreads_or(bad);
+                    if (bad) { cov = true; break; }
+                    ag_coop_table_pass2(E, cf, tn, Tab, S.scr, tid);
+                    __syncthreads();
+                    if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
+                    if (!conv) {
+                        const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
+                        const double vp[3] = {S.vs[0][lane], S.vs[1][lane], S.vs[2][lane]};
+                        double acc[3];
+                        if (NV > 0) {
+                            double J[3][6];
+                            ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
+                            for (int a = 0; a < 3; a++)
+                                for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
+                        } else {
+                            ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                        }
+                        S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
+                        if (wid == 0) n_ev++;
+                    }
+                    __syncthreads();
+                    if (!conv) {
+                        for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                            double at;
+                            if (comp < 3) {
+                                at = ((S.pa[3][comp][lane] + S.pa[2][comp][lane]) + S.pa[1][comp][lane]) + S.pa[0][comp][lane];
+                            } else {
+                                const int q = (comp - 3) / 3, a = (comp - 3) % 3;
+                                double Jr[6];
+                                for (int b = 0; b < 6; b++)
+                                    Jr[b] = ((S.pj[3][6 * a + b][lane] + S.pj[2][6 * a + b][lane]) + S.pj[1][6 * a + b][lane]) +
+                                            S.pj[0][6 * a + b][lane];
+                                const double* dxq = &S.xs[3 + 3 * q][0];
+                                const double* dvq = &S.vs[3 + 3 * q][0];
+                                double s = Jr[0] * dxq[lane];
+                                s = fma(Jr[1], dxq[32 + lane], s); s = fma(Jr[2], dxq[64 + lane], s);
+                                s = fma(Jr[3], dvq[lane], s); s = fma(Jr[4], dvq[32 + lane], s); s = fma(Jr[5], dvq[64 + lane], s);
+                                at = s;
+                            }
+                            double gn = (at - W(W_A0, comp)) * ag_ias.rrinv[n][0];
+                            for (int j = 1; j < n; j++) gn = (gn - W(W_G + j - 1, comp)) * ag_ias.rrinv[n][j];
+                            const double delta = gn - W(W_G + n - 1, comp);
+                            W(W_G + n - 1, comp) = gn;
+                            for (int k = 0; k < n - 1; k++) W(W_B + k, comp) = fma(delta, ag_ias.c[n - 1][k], W(W_B + k, comp));
+                            W(W_B + n - 1, comp) += delta;
+                            if (n == 7 && comp < 3) {
+                                const double aa = fabs(at), db = fabs(delta);
+                                S.ra[comp][lane] = ag_isnormal_pos(aa) ? aa : 0.0;
+                                S.rdb[comp][lane] = ag_isnormal_pos(db) ? db : 0.0;
+                            }
+                        }
+                    }
+                }
+                if (cov) break;
+                __syncthreads();
+                if (!conv) {
+                    double maxa = 0.0, maxdb = 0.0;
+                    for (int k = 0; k < 3; k++) {
+                        if (S.ra[k][lane] > maxa) maxa = S.ra[k][lane];
+                        if (S.rdb[k][lane] > maxdb) maxdb = S.rdb[k][lane];
+                    }
+                    ma7 = maxa;
+                    const double pc_err = maxdb / maxa;
+                    conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+                    if (conv) { it_lane = iters; if (wid == 0) n_it += (unsigned long long)iters; }
+                    else pc_last = pc_err;
+                }
+                if (__all_sync(AG_FULL, conv)) break;
+                iters++;
+            }
+            if (cov) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            if (warm && live) {
+                if (w_applied) { wl_sum_l += it_lane; wl_n_l++; }
+                else if (w_probe) {
+                    wl_sum_p += it_lane; wl_n_p++;
+                    /* the plain predictor converges faster for this particle: fall back */
+                    if (wl_n_p >= 4 && wl_n_l >= 8 && (long long)wl_sum_l * wl_n_p > (long long)wl_sum_p * wl_n_l) {
+                        wl_on = false;
+                        if (wid == 0) n_wfall++;
+                    }
+                }
+            }
+            /* ---- step-size control: each lane's choice, the group takes the smallest */
+            if (live && wid >= 1) {
+                const double bb = fabs(W(W_B + 6, wid - 1));
+                S.rb6[wid - 1][lane] = ag_isnormal_pos(bb) ? bb : 0.0;
+            }
+            __syncthreads();
+            double dt_new_l = 1e300, dt_nocap_l = 1e300;
+            bool rej_l = false;
+            if (A.epsilon > 0.0 && live) {
+                double mb = 0.0;
+                for (int k = 0; k < 3; k++)
+                    if (S.rb6[k][lane] > mb) mb = S.rb6[k][lane];
+                const double err = mb / ma7;
+                const double safety = 0.25;
+                double dn;
+                if (ag_isnormal_pos(err)) dn = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
+                else dn = hstep / safety;
+                if (fabs(dn) < A.min_dt) dn = copysign(A.min_dt, dn);
+                dt_nocap_l = fabs(dn);
+                const double ratio = dn / hstep;
+                if (fabs(ratio) < safety) rej_l = true;
+                else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
+                dt_new_l = fabs(dn);
+            }
+            if (live && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
+                /* step underflow: this lane's particle is hitting a body; it stops
+                 * (state of the step start) and the group goes on without it */
+                pstat = AG_ST_UNDERFLOW;
+                finish_now = true;
+                rej_l = false;
+                dt_new_l = 1e300;
+                dt_nocap_l = 1e300;
+            }
+            if (__any_sync(AG_FULL, finish_now && pstat == AG_ST_UNDERFLOW)) {
+                if (!__any_sync(AG_FULL, live && !finish_now)) continue;   /* only underflowing lanes left */
+            }
+            double dt_new;
+            if (A.epsilon > 0.0) {
+                dt_new = dir * warp_min(dt_new_l);
+                /* a step shortened to land on a lane's t_end does not shrink the
+                 * group's step beyond what the error control asks for */
+                if (last_group) dt_new = dir * fmin(fabs(dt), fmax(fabs(dt_new), warp_min(dt_nocap_l)));
+            } else {
+                dt_new = dt;            /* fixed step */
+            }
+            const bool reject = __any_sync(AG_FULL, rej_l);
+            if (reject) {
+                if (live) {
+                    if (wid == 0) n_rej++;
+                    for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                        if (dtls != 0.0) ag_predict_next_comp<C>(W, comp, dt_new / dtls);
+                        else
+                            for (int k = 0; k < 7; k++) { W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; }
+                    }
+                }
+                dt = dt_new;
+                continue;
+            }
+            /* ---- log (features, target) pairs of accepted steps: target =
+             * (b_conv - b_pred) / kappa with b_pred = e + (br - er), the plain prediction */
+            if (logp) {
+                const bool lg = live && WS.valid[lane] && (steps % A.log_every) == 0;
+                if (lg && wid >= 1)
+                    for (int k = 0; k < 7; k++) {
+                        const int c = wid - 1;
+                        const double bp = W(W_E + k, c) + (W(W_BR + k, c) - W(W_ER + k, c));
+                        WS.tgt[k][c][lane] = (float)((W(W_B + k, c) - bp) / WS.kappa[k][lane]);
+                    }
+                __syncthreads();
+                if (lg && wid == 0) {
+                    bool fin = true;
+                    for (int k = 0; k < 7; k++)
+                        for (int c = 0; c < 3; c++) fin = fin && isfinite(WS.tgt[k][c][lane]) && fabsf(WS.tgt[k][c][lane]) < 1e6f;
+                    if (fin) {
+                        const int row = atomicAdd(A.log_count, 1);
+                        if (row < A.log_cap) {
+                            for (int i = 0; i < AG_MLP_IN; i++) A.log_x[(size_t)row * AG_MLP_IN + i] = WS.xf[lane][i];
+                            for (int k = 0; k < 7; k++)
+                                for (int c = 0; c < 3; c++) A.log_t[(size_t)row * AG_MLP_OUT + 3 * k + c] = WS.tgt[k][c][lane];
+                        }
+                    }
+                }
+            }
+            /* ---- accept */
+            if (live) {
+                if (wid == 0) n_acc++;
+                const double h2 = hstep * hstep;
+                for (int comp = 0; comp < C; comp++) {
+                    if (ag_coop_owner(comp) != wid) continue;
+                    double b[7];
+#pragma unroll
+                    for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
+                    const double a0 = W(W_A0, comp);
+                    double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
+                    ix = fma(ix, h2, W(W_V0, comp) * hstep);
+                    double y = ix + W(W_XC, comp);
+                    const double x0 = W(W_X0, comp);
+                    double s = x0 + y;
+                    W(W_XC, comp) = y - (s - x0);
+                    W(W_X0, comp) = s;
+                    double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
+                    iv = iv * hstep;
+                    y = iv + W(W_VC, comp);
+                    const double v0 = W(W_V0, comp);
+                    s = v0 + y;
+                    W(W_VC, comp) = y - (s - v0);
+                    W(W_V0, comp) = s;
+#pragma unroll
+                    for (int k = 0; k < 7; k++) { W(W_ER + k, comp) = W(W_E + k, comp); W(W_BR + k, comp) = b[k]; }
+                    ag_predict_next_comp<C>(W, comp, dt_new / hstep);
+                }
+            }
+            {
+                const double y = hstep + tc;
+                const double s = t + y;
+                tc = y - (s - t);
+                t = s;
+            }
+            dtls = hstep;
+            dt = dt_new;
+            steps++;
+            if (last) finish_now = true;
+            if (last_group && live && !last && fabs((tend - t) - tc) == 0.0) finish_now = true;
+            if (A.max_steps > 0 && steps >= A.max_steps && live && !finish_now) { pstat = AG_ST_BUDGET; finish_now = true; }
+        }
+    }
+    if (wid == 0) {
+        atomicAdd(&A.counters[0], n_acc);
+        atomicAdd(&A.counters[1], n_rej);
+        atomicAdd(&A.counters[2], n_ev);
+        atomicAdd(&A.counters[3], n_it);
+        atomicAdd(&A.counters[4], n_wused);
+        atomicAdd(&A.counters[5], n_wfall);
+    }
+}
+
+int ag_coop_max_slots(int nv) {
+    int dev = 0, sms = 0, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (nv == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false>, 128, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false>, 128, 0);
+    if (bps < 1) bps = 1;
+    return sms * bps * 32;
+}
+
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s) {
+    int e = ag_ias_tables_init();
+    if (e) return e;
+    const int blocks = (a.nslots + 31) / 32;
+    if (nv == 6) {
+        ag_k_coop<6, false><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+    } else if (a.mlp || a.log_x) {
+        const int dyn = (int)sizeof(AgWarmSmem);
+        cudaError_t r = cudaFuncSetAttribute(ag_k_coop<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+        if (r != cudaSuccess) return (int)r;
+        ag_k_coop<0, true><<<blocks, 128, dyn, s>>>(E.self_dev, c, a);
+    } else {
+        ag_k_coop<0, false><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+    }
+    return (int)cudaGetLastError();
+}

@@ -47,6 +47,12 @@ struct AgBatchArgs {
     const int* grp_start;
     const int* grp_size;
     int n_groups;
+    /* learned warm start (block-cooperative kernel, no variational particles) */
+    const struct AgMlpDev* mlp;     /* network for the warm start, or null (plain predictor) */
+    float* log_x;                   /* [log_cap][32] features of logged steps, or null */
+    float* log_t;                   /* [log_cap][21] their targets */
+    int* log_count;                 /* next log row (atomic) */
+    int log_cap, log_every;
 };
 
 /* launchers (kernels_forces.cu, kernels_ias15.cu) */
@@ -60,6 +66,8 @@ int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, 
 int ag_batch_max_slots(int nv, int tpb);
 int ag_group_max_slots(int nv);
 int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
+int ag_coop_max_slots(int nv);
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
 double ag_fp64_probe_gflops(void);
 
 /* shared-step device IAS15 (kernels_shared.cu) */
@@ -76,6 +84,10 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out);
 
 /* 1 when the ephemeris's device view exists (ag_ephem_device will not allocate) */
 int ag_ephem_view_ready(const struct assist_ephem* e);
+
+/* warm-start network (kernels_mlp.cu) */
+const struct AgMlpDev* ag_mlp_device_view(void);
+int ag_mlp_log_config(float** x, float** t, int* cap, int* every, int** count);
 
 /* library error state */
 void ag_set_error(const std::string& msg);

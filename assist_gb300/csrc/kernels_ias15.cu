@@ -38,6 +38,7 @@
 #include "ias15_constants.h"
 #include "internal.h"
 #include "warp_table.cuh"
+#include "mlp.cuh"
 
 #define AG_ST_OK 0
 #define AG_ST_COVERAGE 1
@@ -883,3 +884,5 @@ int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, 
     else ag_k_group<0><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
     return (int)cudaGetLastError();
 }
+
+#include "ias15_coop.cuh"

@@ -73,6 +73,27 @@ def algorithmic_flops(pl, ast, pop, stats):
     return flops, per_eval, c
 
 
+def train_warm_start(eph, system, dev, n_train: int = 16384, steps: int = 1500):
+    """Log (features, target) pairs from one plain integration of a separate
+    seeded population of the same mixture and train the warm-start network
+    with the device kernels (outside the timed region)."""
+    import torch
+    from assist_gb300 import synth, warm
+    tp = synth.population(system, "mix", n_train, seed=SEED_POP + 1, t0=T0, log_len=(30.0, 3652.5), nongrav_frac=0.1)
+    t = time.perf_counter()
+    warm.init(SEED_POP)
+    X, T, _ = warm.collect(eph, torch.tensor(tp.t0, device=dev), torch.tensor(tp.t_end, device=dev),
+                           torch.tensor(tp.state, device=dev), params=torch.tensor(tp.params, device=dev),
+                           capacity=1 << 21, every=2)
+    perm = torch.randperm(X.shape[0], device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    X, T = X[perm].contiguous(), T[perm].clamp(-4, 4).contiguous()
+    l0, _ = warm.grad(X[:4096], T[:4096])
+    loss = warm.train(X, T, steps=steps, batch=4096, lr=1e-3, seed=1)
+    torch.cuda.synchronize()
+    return {"pairs": int(X.shape[0]), "train_particles": n_train, "train_steps": steps, "batch": 4096,
+            "loss_initial": l0, "loss_final": loss, "train_s": time.perf_counter() - t}
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
@@ -187,6 +208,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="plain predictor only (no learned warm start)")
     ap.add_argument("--particles", type=int, default=None, help="override the batch size (profiling only)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -208,59 +230,76 @@ def main():
     pl, ast, system, pop = make_inputs(tmp)
     eph = Ephem(pl, ast)
     dev = torch.device("cuda", local)
-    opts = batch.options()
     t0 = torch.tensor(pop.t0, device=dev)
     te = torch.tensor(pop.t_end, device=dev)
     st0 = torch.tensor(pop.state, device=dev)
     prm = torch.tensor(pop.params, device=dev)
-    st = st0.clone()
-    status = torch.zeros(N_PARTICLES, dtype=torch.int32, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
-    pdays = float(np.abs(pop.t_end - pop.t0).sum())
-    for _ in range(args.warmup):
-        st.copy_(st0)
-        batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=opts, stream=stream)
-    torch.cuda.synchronize()
+    plain_opts = batch.options(group_steps=2, warm_start=0)
+    warm_info = None
+    if not args.no_warm:
+        warm_info = train_warm_start(eph, system, dev)
+    opts = batch.options(group_steps=2, warm_start=0 if args.no_warm else 1)
+
+    def timed(o):
+        st = st0.clone()
+        status = torch.zeros(N_PARTICLES, dtype=torch.int32, device=dev)
+        for _ in range(args.warmup):
+            st.copy_(st0)
+            batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=o, stream=stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        evs, acc = [], None
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            st.copy_(st0)
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s = batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=o, stream=stream)
+            e1.record(stream)
+            evs.append((e0, e1))
+            if acc is None:
+                acc = dict(s)
+            else:
+                for k in ("steps_accepted", "steps_rejected", "force_evals", "pc_iterations", "kernel_ms",
+                          "warm_start_used", "warm_start_fallback"):
+                    acc[k] += s[k]
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        wall = time.perf_counter() - wall0
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, acc, status.cpu().numpy(), st, wall
+
+    plain = None
+    if not args.no_warm:
+        pms, pacc, pstat, pst, _ = timed(plain_opts)
+        pdone = pstat == 0
+        plain = {"value": world * float(np.abs(pop.t_end - pop.t0)[pdone].sum()) * args.steps / (pms / 1e3),
+                 "unit": UNIT, "ms_per_step": pms / args.steps,
+                 "iterations_per_step": pacc["pc_iterations"] / max(pacc["steps_accepted"] + pacc["steps_rejected"], 1),
+                 "force_evals": pacc["force_evals"] // args.steps}
     clocks = ClockSampler(local)
     clocks.start()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    evs = []
-    stats_acc = None
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        st.copy_(st0)
-        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        s = batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=opts, stream=stream)
-        e1.record(stream)
-        evs.append((e0, e1))
-        if stats_acc is None:
-            stats_acc = dict(s)
-        else:
-            for k in ("steps_accepted", "steps_rejected", "force_evals", "pc_iterations", "kernel_ms"):
-                stats_acc[k] += s[k]
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    wall = time.perf_counter() - wall0
+    ms, stats_acc, st_host, st_dev, wall = timed(opts)
     clocks.stop()
-    ms = sum(a.elapsed_time(b) for a, b in evs)
     # particle-days of the particles that reached t_end (a particle that hits a
     # body stops with status 4 and its span is not counted)
-    st_host = status.cpu().numpy()
     done = st_host == 0
     pdays = float(np.abs(pop.t_end - pop.t0)[done].sum())
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     bad = int((~done).sum())
     status_counts = {str(k): int(v) for k, v in zip(*np.unique(st_host, return_counts=True))}
     value = world * pdays * args.steps / (ms / 1e3)
+    if plain is not None:
+        plain["max_end_state_difference_au"] = float(np.abs(st_dev.cpu().numpy()[done, :3] - pst.cpu().numpy()[done, :3]).max())
     # e2e through the host-array C entry point
     e2e = None
     if rank == 0:
@@ -289,7 +328,9 @@ def main():
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .440/SPK ephemeris, seeded population)",
             "config": {"workload": "batched-65536-mixture-logU30d-10yr", "n_particles": N_PARTICLES,
                        "particle_days_per_step": pdays, "epsilon": 1e-9, "forces": "0x7F (ASSIST default)",
-                       "warm_start": "plain predictor", "l2": "flushed (256 MB write) between steps",
+                       "warm_start": "plain predictor" if args.no_warm else
+                       "learned (network trained in this run on a separate seeded population)",
+                       "l2": "flushed (256 MB write) between steps", "kernel": "block-cooperative groups (group_steps=2)",
                        "parallelism": "dp%d (independent batches, no collective)" % world},
             "gpu_launches": args.steps, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(),
@@ -298,7 +339,9 @@ def main():
                       "force_evals": stats_acc["force_evals"] // args.steps,
                       "iterations_per_step": stats_acc["pc_iterations"] / max(stats_acc["steps_accepted"] +
                                                                               stats_acc["steps_rejected"], 1)},
-            "unfinished_particles": bad, "status_counts": status_counts, "wall_s_timed_region": wall}
+            "unfinished_particles": bad, "status_counts": status_counts, "wall_s_timed_region": wall,
+            "plain_ias15": plain, "warm_start": warm_info and dict(warm_info, used=stats_acc["warm_start_used"] // args.steps,
+                                                                   fallback=stats_acc["warm_start_fallback"] // args.steps)}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

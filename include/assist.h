@@ -201,10 +201,13 @@ struct assist_gb300_options {
     double min_dt;          /* IAS15 minimum |dt| (0 => none) */
     double dt0;             /* initial |dt| (REBOUND default 0.001 day) */
     int max_steps;          /* per-particle step budget, 0 => unlimited */
-    int warm_start;         /* 0 plain predictor, 1 learned warm start (needs a loaded MLP) */
+    int warm_start;         /* 0 plain predictor; 1 learned warm start (needs a network, see
+                               assist_gb300_warm_*; group_steps = 2 and no variational particles) */
     int threads_per_block;  /* 0 => autotuned */
-    int group_steps;        /* 1 (default): up to 32 particles with the same start time and
-                               similar orbital timescale share each adaptive step (one warp);
+    int group_steps;        /* 1: up to 32 particles with the same start time and similar
+                               orbital timescale share each adaptive step (one warp);
+                               2 (default): the same groups, each integrated by a 128-thread
+                               block whose four warps split every force evaluation;
                                0: every particle takes its own adaptive step */
     double dt_floor;        /* a particle whose adaptive step falls below this |dt| (days)
                                stops with ASSIST_GB300_STEP_UNDERFLOW (an impact: any orbit
@@ -282,6 +285,34 @@ int assist_gb300_integrate_batch_device_static(const struct assist_ephem* ephem,
                                                const double* d_t0, const double* d_t_end, double* d_state,
                                                const double* d_params, int* d_status, void* stream,
                                                struct assist_gb300_batch_stats* stats);
+
+/* ---- Learned IAS15 warm start (no counterpart in the reference).
+ * One network per process: 32 step features -> 256 -> 256 -> 21 corrections
+ * of IAS15's predicted b coefficients (GELU, weights [out][in]; the flat
+ * parameter order is W1, b1, W2, b2, W3, b3).  Training is FP32 on the
+ * device; inference is BF16 on the tensor cores inside the batched kernel,
+ * where IAS15's own convergence test and error estimate still decide and the
+ * plain predictor takes over for a particle whose learned starts converge
+ * slower.  Device pointers are float32, row-major. */
+int assist_gb300_warm_n_params(void);
+int assist_gb300_warm_init(unsigned long long seed);                 /* random weights, zero biases */
+int assist_gb300_warm_set_params(const float* params, int n);        /* host array of n_params */
+int assist_gb300_warm_get_params(float* params, int n);
+/* Loss 1/(2n) sum (Y - T)^2 over n pairs and its gradient (host array of n_params). */
+int assist_gb300_warm_grad(const float* d_x, const float* d_t, int n, float* grad, double* loss);
+/* One Adam step (0.9, 0.999, 1e-8) with a given gradient (host array). */
+int assist_gb300_warm_adam_step(const float* grad, float lr);
+/* `steps` Adam steps on minibatches of `batch` consecutive pairs chosen at
+ * random (seeded) from n pairs; *loss = last minibatch loss. */
+int assist_gb300_warm_train(const float* d_x, const float* d_t, int n, int steps, int batch, float lr,
+                            unsigned long long seed, double* loss);
+/* BF16 tensor-core inference of n feature rows into d_y [n][21]. */
+int assist_gb300_warm_infer(const float* d_x, int n, float* d_y);
+/* Log (features, target) pairs of every `every`-th accepted step in the next
+ * batched integrations (group_steps = 2, n_var = 0) into d_x [cap][32],
+ * d_t [cap][21]; NULL stops logging.  Resets the count. */
+int assist_gb300_warm_set_log(float* d_x, float* d_t, int capacity, int every);
+int assist_gb300_warm_log_count(void);
 
 /* One force evaluation for n particles at per-particle times t[i] (device
  * pointers): acc[3i..3i+2] = a(x_i, v_i, t_i) for the force model in `opt`.

@@ -14,7 +14,7 @@ def _eph(paths):
     return Ephem(*paths)
 
 
-@pytest.mark.parametrize("group_steps", [0, 1])
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
 def test_batch_vs_oracle_mixture(synth_files, group_steps):
     """Independent steps (group_steps=0) reproduce the oracle's per-particle
     integrations step for step; warp-synchronous groups (1) take the group's
@@ -85,7 +85,7 @@ def test_batch_roundtrip(synth_files):
     assert np.abs(back[:, :3] - pop.state[:, :3]).max() * AU_M < 1.0      # < 1 m over 600 days
 
 
-@pytest.mark.parametrize("group_steps", [0, 1])
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
 def test_batch_error_vs_double_double(synth_files, group_steps):
     from assist_gb300 import batch, synth
     from tests.oracle_py import Oracle
@@ -98,7 +98,7 @@ def test_batch_error_vs_double_double(synth_files, group_steps):
         assert np.abs(out[i, :3] - dd[0, :3]).max() < 1e-11
 
 
-@pytest.mark.parametrize("group_steps", [0, 1])
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
 def test_batch_coverage_status(synth_files, group_steps):
     from assist_gb300 import batch, synth
     pl, ast, system = synth_files
@@ -162,7 +162,7 @@ def test_shared_step_roundtrip(synth_files):
     ex.detach(sim); sim.free()
 
 
-@pytest.mark.parametrize("group_steps", [0, 1])
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
 def test_batch_fixed_step_bitwise(synth_files, group_steps):
     """epsilon = 0 (fixed dt): the device reproduces the oracle bit for bit."""
     from assist_gb300 import batch, synth

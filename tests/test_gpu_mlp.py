@@ -1,0 +1,109 @@
+"""Warm-start network on the device: the hand-written FP32 backward pass and
+Adam against the CPU oracle, BF16 tensor-core inference against the oracle's
+forward pass, and the learned warm start inside the batched IAS15 (same end
+states as the plain predictor; iterations per step reported)."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.tensor(np.asarray(a, np.float32), device="cuda")
+
+
+def test_device_gradient_matches_oracle():
+    from assist_gb300 import warm
+    rng = np.random.default_rng(11)
+    p = M.init(4).astype(np.float32)
+    # a non-trivial last layer so every gradient block is exercised
+    pp = M.unpack(p.astype(np.float64)); pp["W3"] = rng.standard_normal(pp["W3"].shape) * 0.05
+    p = M.pack(pp).astype(np.float32)
+    X = rng.standard_normal((300, M.N_IN)).astype(np.float32)
+    T = (rng.standard_normal((300, M.N_OUT)) * 0.2).astype(np.float32)
+    warm.set_params(p)
+    loss, g = warm.grad(_dev(X), _dev(T))
+    L, gref = M.loss_and_grad(p.astype(np.float64), X.astype(np.float64), T.astype(np.float64))
+    assert abs(loss - L) <= 1e-5 * L
+    for name, _ in M.PARAM_SHAPES:
+        a, b = M.unpack(g)[name], M.unpack(gref)[name]
+        # FP32 accumulation over 300 rows: error ~1e-6 of the block's scale
+        assert np.abs(a - b).max() <= 1e-4 * np.abs(b).max() + 1e-9, name
+
+
+def test_device_adam_matches_oracle():
+    from assist_gb300 import warm
+    rng = np.random.default_rng(2)
+    p = M.init(9).astype(np.float32)
+    warm.set_params(p)
+    m = np.zeros(p.size); v = np.zeros(p.size); q = p.astype(np.float64)
+    for step in range(1, 4):
+        g = (rng.standard_normal(p.size) * 1e-2).astype(np.float32)
+        warm.adam_step(g, 1e-3)
+        q, m, v = M.adam_step(q, g.astype(np.float64), m, v, step, 1e-3)
+    assert np.abs(warm.get_params() - q).max() <= 1e-6
+
+
+def test_bf16_inference_matches_oracle_forward():
+    from assist_gb300 import warm
+    rng = np.random.default_rng(3)
+    p = M.init(6).astype(np.float32)
+    pp = M.unpack(p.astype(np.float64)); pp["W3"] = rng.standard_normal(pp["W3"].shape) * 0.1
+    pp["b1"] = rng.standard_normal(256) * 0.1; pp["b3"] = rng.standard_normal(21) * 0.1
+    p = M.pack(pp).astype(np.float32)
+    warm.set_params(p)
+    X = rng.uniform(-1, 1, (100, M.N_IN)).astype(np.float32)      # 100 rows: a ragged last block of 32
+    Y = warm.infer(_dev(X)).cpu().numpy()
+    Yref, _ = M.forward(p.astype(np.float64), X.astype(np.float64))
+    # BF16 inputs and weights (8-bit mantissa), FP32 accumulation
+    assert np.abs(Y - Yref).max() <= 3e-2 * np.abs(Yref).max()
+
+
+def test_learned_warm_start_in_batched_ias15(synth_files, capsys):
+    import torch
+    from assist_gb300 import Ephem, batch, synth, warm
+    pl, ast, system = synth_files
+    eph = Ephem(pl, ast)
+    dev = torch.device("cuda", 0)
+
+    def tens(pop):
+        return (torch.tensor(pop.t0, device=dev), torch.tensor(pop.t_end, device=dev),
+                torch.tensor(pop.state, device=dev), torch.tensor(pop.params, device=dev))
+
+    train_pop = synth.population(system, "mix", 4096, seed=31, t0=8000.0, log_len=(100.0, 900.0), nongrav_frac=0.1)
+    t0, te, st, prm = tens(train_pop)
+    warm.init(7)
+    X, T, _ = warm.collect(eph, t0, te, st, params=prm, capacity=1 << 19, every=1)
+    assert X.shape[0] > 10000 and torch.isfinite(X).all() and torch.isfinite(T).all()
+    perm = torch.randperm(X.shape[0], device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    X, T = X[perm].contiguous(), T[perm].clamp(-4, 4).contiguous()
+    l0, _ = warm.grad(X[:4096], T[:4096])
+    loss = warm.train(X, T, steps=600, batch=2048, lr=1e-3, seed=1)
+    assert loss < l0
+
+    pop = synth.population(system, "mix", 2048, seed=32, t0=8000.0, log_len=(100.0, 900.0), nongrav_frac=0.1)
+    t0, te, s0, prm = tens(pop)
+    res = {}
+    for w in (0, 1):
+        st = s0.clone(); status = torch.zeros(len(pop.t0), dtype=torch.int32, device=dev)
+        stats = batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status,
+                                             opts=batch.options(group_steps=2, warm_start=w))
+        torch.cuda.synchronize()
+        res[w] = (st.cpu().numpy(), status.cpu().numpy(), stats)
+    (xp, sp, stp), (xl, sl, stl) = res[0], res[1]
+    assert np.array_equal(sp, sl)
+    ok = sp == 0
+    # same end states as the plain predictor within the 1e-9 AU bar
+    assert np.abs(xl[ok, :3] - xp[ok, :3]).max() < 1e-9
+    assert stl["warm_start_used"] > 0
+    it_p = stp["pc_iterations"] / max(1, stp["steps_accepted"] + stp["steps_rejected"])
+    it_l = stl["pc_iterations"] / max(1, stl["steps_accepted"] + stl["steps_rejected"])
+    with capsys.disabled():
+        print("\nwarm start: pairs %d, loss %.4g -> %.4g; iterations/step plain %.4f learned %.4f; evals %d -> %d; "
+              "used %d fallback %d" % (X.shape[0], l0, loss, it_p, it_l, stp["force_evals"], stl["force_evals"],
+                                       stl["warm_start_used"], stl["warm_start_fallback"]))
+    # the fallback keeps the learned start from costing more than the plain predictor
+    assert it_l <= it_p * 1.05

@@ -45,7 +45,7 @@ class Options(ctypes.Structure):
                 ("alpha", c_double), ("nk", c_double), ("nm", c_double), ("nn", c_double), ("r0", c_double),
                 ("epsilon", c_double), ("min_dt", c_double), ("dt0", c_double), ("max_steps", c_int),
                 ("warm_start", c_int), ("threads_per_block", c_int), ("group_steps", c_int),
-                ("dt_floor", c_double)]
+                ("dt_floor", c_double), ("group_order", c_int)]
 
 
 class BatchStats(ctypes.Structure):

@@ -352,16 +352,13 @@ __device__ __forceinline__ void ag_term_sun_h(const DevEphem& E, const ForceCfg&
     }
 }
 
-/* Einstein-Infeld-Hoffmann (PPN, beta = gamma = 1) over the first
- * gr_eih_sources planets; dx..ri: separations from all eleven planets. */
-template <class Bodies, bool JAC>
-__device__ __forceinline__ void ag_term_eih(const Bodies& B, const DevEphem& E, const ForceCfg& c,
-                                            const PlanetState& P, const double* dx, const double* dy, const double* dz,
-                                            const double* ri, const double* v, const double* vo, const double* ao,
-                                            double& ax, double& ay, double& az, double (*J)[6]) {
-    const double oc2 = E.over_c_squared;
-    double term0 = 0.0;
-    double g0[3] = {0.0, 0.0, 0.0};              /* sum_k GM_k d_ik / r_ik^3 (variational) */
+/* EIH sums over all eleven planets that do not depend on the source:
+ * sum_k GM_k / r_ik and (variational) sum_k GM_k d_ik / r_ik^3. */
+template <bool JAC>
+__device__ __forceinline__ void ag_eih_planet_sums(const DevEphem& E, const double* dx, const double* dy,
+                                                   const double* dz, const double* ri, double& term0, double* g0) {
+    term0 = 0.0;
+    g0[0] = g0[1] = g0[2] = 0.0;
 #pragma unroll
     for (int k = 0; k < AG_NPL; k++) {
         const double gri = E.gm[k] * ri[k];
@@ -371,20 +368,26 @@ __device__ __forceinline__ void ag_term_eih(const Bodies& B, const DevEphem& E, 
             g0[0] = fma(f, dx[k], g0[0]); g0[1] = fma(f, dy[k], g0[1]); g0[2] = fma(f, dz[k], g0[2]);
         }
     }
+}
+
+/* Einstein-Infeld-Hoffmann (PPN, beta = gamma = 1) over the first
+ * gr_eih_sources planets, given the planet sums above; sep(j, dj, rj) gives
+ * the separation from source j and its inverse length. */
+template <class Bodies, bool JAC, class Sep>
+__device__ __forceinline__ void ag_term_eih_core(const Bodies& B, const DevEphem& E, const ForceCfg& c,
+                                                 const PlanetState& P, double term0, const double* g0, Sep sep,
+                                                 const double* v, const double* vo, const double* ao, double& ax,
+                                                 double& ay, double& az, double (*J)[6]) {
+    const double oc2 = E.over_c_squared;
     term0 *= -4.0 * oc2;
     const double vi2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
     double t7[3] = {0.0, 0.0, 0.0}, t8[3] = {0.0, 0.0, 0.0};
     const int nsrc = c.gr_eih_sources;
 #pragma unroll 1
     for (int j = 0; j < nsrc; j++) {
-        /* select source j's data with static indices (keeps arrays in registers) */
-        double dj[3] = {0.0, 0.0, 0.0}, rj = 0.0, vjb[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-        for (int k = 0; k < AG_NPL; k++)
-            if (k == j) {
-                dj[0] = dx[k]; dj[1] = dy[k]; dj[2] = dz[k]; rj = ri[k];
-                vjb[0] = P.vx[k]; vjb[1] = P.vy[k]; vjb[2] = P.vz[k];
-            }
+        double dj[3], rj;
+        sep(j, dj, rj);
+        const double vjb[3] = {P.vx[j], P.vy[j], P.vz[j]};
         const double GMj = E.gm[j];
         const double pre = GMj * rj * rj * rj;
         const double vj[3] = {vjb[0] - vo[0], vjb[1] - vo[1], vjb[2] - vo[2]};
@@ -441,6 +444,25 @@ __device__ __forceinline__ void ag_term_eih(const Bodies& B, const DevEphem& E, 
     ax += t7[0] * oc2 + t8[0] * oc2;
     ay += t7[1] * oc2 + t8[1] * oc2;
     az += t7[2] * oc2 + t8[2] * oc2;
+}
+
+/* EIH with the separations from all eleven planets in arrays. */
+template <class Bodies, bool JAC>
+__device__ __forceinline__ void ag_term_eih(const Bodies& B, const DevEphem& E, const ForceCfg& c,
+                                            const PlanetState& P, const double* dx, const double* dy, const double* dz,
+                                            const double* ri, const double* v, const double* vo, const double* ao,
+                                            double& ax, double& ay, double& az, double (*J)[6]) {
+    double term0, g0[3];
+    ag_eih_planet_sums<JAC>(E, dx, dy, dz, ri, term0, g0);
+    auto sep = [&](int j, double* dj, double& rj) {
+        /* select source j's data with static indices (keeps arrays in registers) */
+        dj[0] = dj[1] = dj[2] = 0.0;
+        rj = 0.0;
+#pragma unroll
+        for (int k = 0; k < AG_NPL; k++)
+            if (k == j) { dj[0] = dx[k]; dj[1] = dy[k]; dj[2] = dz[k]; rj = ri[k]; }
+    };
+    ag_term_eih_core<Bodies, JAC>(B, E, c, P, term0, g0, sep, v, vo, ao, ax, ay, az, J);
 }
 
 /* GR potential (Nobili & Roxburgh); p, rinv: heliocentric separation. */

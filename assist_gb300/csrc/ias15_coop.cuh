@@ -279,6 +279,64 @@ __device__ __forceinline__ double ag_nearest_planet(const AgTable& T, double x, 
     return sqrt(m);
 }
 
+/* Node-0 part of the learned warm start for one group (all threads of the
+ * block call it): owners publish (br - er) and |b_pred|, warp 0 forms the
+ * features, the block runs the network, owners add kappa_k y_kc to b.  Kept
+ * out of line so the plain kernel's register allocation is not shaped by it. */
+__device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws, int nslots, int slot, AgWarmSmem& WS,
+                                               const AgTable& Tab, int lane, int wid, bool live, bool warm, bool wl_on,
+                                               double hstep, double dtls, long long steps, bool& w_applied,
+                                               bool& w_probe, unsigned long long& n_wused,
+                                               unsigned long long& n_wfall) {
+    const Ws<3> W{ws, nslots, slot};
+    if (live && wid >= 1)
+        for (int k = 0; k < 7; k++) {
+            WS.corr[k][wid - 1][lane] = W(W_BR + k, wid - 1) - W(W_ER + k, wid - 1);
+            WS.bpa[k][wid - 1][lane] = (float)fabs(W(W_B + k, wid - 1));
+        }
+    __syncthreads();
+    if (wid == 0) {
+        bool ok = false;
+        if (live) {
+            double corr[7][3], kap[7];
+            float bpa[7][3], x[AG_MLP_IN];
+            for (int k = 0; k < 7; k++)
+                for (int c = 0; c < 3; c++) { corr[k][c] = WS.corr[k][c][lane]; bpa[k][c] = WS.bpa[k][c][lane]; }
+            const double x0 = W(W_X0, 0), y0 = W(W_X0, 1), z0 = W(W_X0, 2);
+            const double rx = sqrt(fma(x0, x0, fma(y0, y0, z0 * z0)));
+            ok = ag_warm_features(corr, bpa, hstep, dtls, rx, ag_nearest_planet(Tab, x0, y0, z0), x, kap);
+            for (int k = 0; k < 7; k++) WS.kappa[k][lane] = kap[k];
+            for (int i = 0; i < AG_MLP_IN; i++) { WS.xf[lane][i] = x[i]; WS.M.X[lane][i] = __float2bfloat16_rn(x[i]); }
+        } else {
+            for (int i = 0; i < AG_MLP_IN; i++) WS.M.X[lane][i] = __float2bfloat16_rn(0.0f);
+        }
+        WS.valid[lane] = ok ? 1 : 0;
+    }
+    __syncthreads();
+    const bool valid = live && WS.valid[lane];
+    w_probe = warm && valid && wl_on && (steps & 7) == 7;
+    const bool want = warm && valid && wl_on && !w_probe;
+    if (__syncthreads_or(want)) {
+        ag_mlp_infer_block(*A.mlp, WS.M, wid, lane);
+        if (want) {
+            bool ok_y = true;
+            for (int o = 0; o < AG_MLP_OUT; o++) {
+                const float y = WS.M.Y[lane][o];
+                ok_y = ok_y && isfinite(y) && fabsf(y) <= AG_MLP_YCLIP;
+            }
+            if (ok_y) {
+                w_applied = true;
+                if (wid >= 1)
+                    for (int k = 0; k < 7; k++)
+                        W(W_B + k, wid - 1) = fma(WS.kappa[k][lane], (double)WS.M.Y[lane][3 * k + wid - 1], W(W_B + k, wid - 1));
+                if (wid == 0) n_wused++;
+            } else if (wid == 0) {
+                n_wfall++;
+            }
+        }
+    }
+}
+
 template <int NV, bool WARM>
 __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
@@ -440,55 +498,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             }
             /* ---- learned warm start: features, BF16 inference, b += kappa y */
             bool w_applied = false, w_probe = false;
-            if (warm || logp) {
-                if (live && wid >= 1)
-                    for (int k = 0; k < 7; k++) {
-                        WS.corr[k][wid - 1][lane] = W(W_BR + k, wid - 1) - W(W_ER + k, wid - 1);
-                        WS.bpa[k][wid - 1][lane] = (float)fabs(W(W_B + k, wid - 1));
-                    }
-                __syncthreads();
-                if (wid == 0) {
-                    bool ok = false;
-                    if (live) {
-                        double corr[7][3], kap[7];
-                        float bpa[7][3], x[AG_MLP_IN];
-                        for (int k = 0; k < 7; k++)
-                            for (int c = 0; c < 3; c++) { corr[k][c] = WS.corr[k][c][lane]; bpa[k][c] = WS.bpa[k][c][lane]; }
-                        const double x0 = W(W_X0, 0), y0 = W(W_X0, 1), z0 = W(W_X0, 2);
-                        const double rx = sqrt(fma(x0, x0, fma(y0, y0, z0 * z0)));
-                        ok = ag_warm_features(corr, bpa, hstep, dtls, rx, ag_nearest_planet(Tab, x0, y0, z0), x, kap);
-                        for (int k = 0; k < 7; k++) WS.kappa[k][lane] = kap[k];
-                        for (int i = 0; i < AG_MLP_IN; i++) { WS.xf[lane][i] = x[i]; WS.M.X[lane][i] = __float2bfloat16_rn(x[i]); }
-                    } else {
-                        for (int i = 0; i < AG_MLP_IN; i++) WS.M.X[lane][i] = __float2bfloat16_rn(0.0f);
-                    }
-                    WS.valid[lane] = ok ? 1 : 0;
-                }
-                __syncthreads();
-                const bool valid = live && WS.valid[lane];
-                w_probe = valid && wl_on && (steps & 7) == 7;
-                const bool want = valid && wl_on && !w_probe;
-                if (__syncthreads_or(want)) {
-                    ag_mlp_infer_block(*A.mlp, WS.M, wid, lane);
-                    if (want) {
-                        bool ok_y = true;
-                        for (int o = 0; o < AG_MLP_OUT; o++) {
-                            const float y = WS.M.Y[lane][o];
-                            ok_y = ok_y && isfinite(y) && fabsf(y) <= AG_MLP_YCLIP;
-                        }
-                        if (ok_y) {
-                            w_applied = true;
-                            if (wid >= 1)
-                                for (int k = 0; k < 7; k++)
-                                    W(W_B + k, wid - 1) = fma(WS.kappa[k][lane], (double)WS.M.Y[lane][3 * k + wid - 1],
-                                                              W(W_B + k, wid - 1));
-                            if (wid == 0) n_wused++;
-                        } else if (wid == 0) {
-                            n_wfall++;
-                        }
-                    }
-                }
-            }
+            if (warm || logp)
+                ag_coop_warm_start(A, W.w, A.nslots, slot, WS, Tab, lane, wid, live, warm, wl_on, hstep, dtls, steps,
+                                   w_applied, w_probe, n_wused, n_wfall);
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
                     if (ag_coop_owner(comp) != wid) continue;

@@ -1,19 +1,24 @@
 """Benchmark: particle-days/s of the batched device IAS15 (FP64) on GB300.
 
-Workload (the batched configuration of ASSIST's test-particle path):
-65,536 independent particles, each with its own adaptive IAS15 step
-(epsilon 1e-9) and its own integration length ~ logU[30 d, 10 yr]; mixture
-40% main belt, 30% NEO, 20% Jupiter-Trojan-like, 10% trans-Neptunian; 10% with
-Marsden non-gravitational A1, A2 ~ +-logU[1e-12, 1e-9] AU/d^2; full ASSIST force
+Workload (the learned-warm-start evaluation configuration of ASSIST's
+test-particle path): 262,144 independent particles of a 40% main-belt, 30%
+NEO, 20% Jupiter-Trojan-like, 10% trans-Neptunian mixture (10% with Marsden
+non-gravitational A1, A2 ~ +-logU[1e-12, 1e-9] AU/d^2), each integrated one
+year with its own adaptive IAS15 steps (epsilon 1e-9), full ASSIST force
 model (Sun, planets, 16 asteroids, Earth J2-J4, Sun J2, EIH GR).  Ephemeris:
 seeded synthetic .440 + 16-asteroid SPK (the JPL files are not available).
+The warm-start network is trained in the run, outside the timed region, on
+(features, target) pairs logged from a separate 65,536-particle population
+of the same mixture with lengths ~ logU[30 d, 10 yr].
 
 One step = one pass of the hot path over the whole batch: every particle
 integrated from t0 to its t_end by the persistent kernel.
 
-  value : particle-days/s with inputs resident in HBM, CUDA events around the
-          kernel on its stream, L2 flushed (256 MB write) between steps.
-  e2e   : the same through the public host-array C entry point
+  value : particle-days/s of the default path (plain IAS15 predictor) with
+          inputs resident in HBM, CUDA events around the kernel on its
+          stream, L2 flushed (256 MB write) between steps.
+  learned_warm_start : the same with the learned warm start, timed beside it.
+  e2e   : the default path through the public host-array C entry point
           assist_gb300_integrate_batch (H2D + kernel + D2H in the timed region).
   roofline : FP64 pipe; achieved = algorithmic FP64 flops (oracle op count per
           force evaluation x evaluations + IAS15 bookkeeping) / kernel time;
@@ -23,7 +28,7 @@ integrated from t0 to its t_end by the persistent kernel.
 
 --impl reference times that CPU path alone (the reference arm).
 Multi-GPU (torchrun): weak scaling, each rank integrates its own batch of the
-same size; no collective on the data path (end-state gather only).
+same size; no collective on the data path.
 """
 from __future__ import annotations
 
@@ -41,10 +46,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_PARTICLES = 65536
+N_PARTICLES = 262144          # evaluation population, one year each
+N_TRAIN = 65536               # pair-logging population, lengths logU[30 d, 10 yr]
+LENGTH = 365.25
 SEED_EPHEM = 20240611
 SEED_POP = 12345
 T0 = 8000.0
+WORKLOAD = "262144-mixture-1yr-learned-warm-start-vs-plain"
 METRIC = "particle-days/s FP64 on 1 GB300: learned-warm-start vs plain IAS15 vs CPU ref"
 UNIT = "particle-days/s"
 
@@ -52,8 +60,7 @@ UNIT = "particle-days/s"
 def make_inputs(tmpdir: str):
     from assist_gb300 import synth
     pl, ast, system = synth.write_ephemeris(tmpdir, seed=SEED_EPHEM, t_beg=T0 - 40.0, t_end=T0 + 3700.0)
-    pop = synth.population(system, "mix", N_PARTICLES, seed=SEED_POP, t0=T0, log_len=(30.0, 3652.5),
-                           nongrav_frac=0.1)
+    pop = synth.population(system, "mix", N_PARTICLES, seed=SEED_POP, t0=T0, length=LENGTH, nongrav_frac=0.1)
     return pl, ast, system, pop
 
 
@@ -73,10 +80,11 @@ def algorithmic_flops(pl, ast, pop, stats):
     return flops, per_eval, c
 
 
-def train_warm_start(eph, system, dev, n_train: int = 16384, steps: int = 1500):
+def train_warm_start(eph, system, dev, n_train: int = N_TRAIN, steps: int = 1500):
     """Log (features, target) pairs from one plain integration of a separate
-    seeded population of the same mixture and train the warm-start network
-    with the device kernels (outside the timed region)."""
+    seeded population of the same mixture (lengths logU[30 d, 10 yr]) and
+    train the warm-start network with the device kernels (outside the timed
+    region)."""
     import torch
     from assist_gb300 import synth, warm
     tp = synth.population(system, "mix", n_train, seed=SEED_POP + 1, t0=T0, log_len=(30.0, 3652.5), nongrav_frac=0.1)
@@ -84,7 +92,7 @@ def train_warm_start(eph, system, dev, n_train: int = 16384, steps: int = 1500):
     warm.init(SEED_POP)
     X, T, _ = warm.collect(eph, torch.tensor(tp.t0, device=dev), torch.tensor(tp.t_end, device=dev),
                            torch.tensor(tp.state, device=dev), params=torch.tensor(tp.params, device=dev),
-                           capacity=1 << 21, every=2)
+                           capacity=5 << 20, every=1)
     perm = torch.randperm(X.shape[0], device=dev, generator=torch.Generator(device=dev).manual_seed(0))
     X, T = X[perm].contiguous(), T[perm].clamp(-4, 4).contiguous()
     l0, _ = warm.grad(X[:4096], T[:4096])
@@ -193,7 +201,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ephemeris + population)",
-            "config": {"workload": "batched-65536-mixture-logU30d-10yr", "n_particles": N_PARTICLES,
+            "config": {"workload": WORKLOAD, "n_particles": N_PARTICLES,
                        "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d random particles of the workload per step (full integrations)" % n},
@@ -236,11 +244,11 @@ def main():
     prm = torch.tensor(pop.params, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
-    plain_opts = batch.options(group_steps=2, warm_start=0)
+    opts = batch.options(group_steps=2, warm_start=0)
+    warm_opts = batch.options(group_steps=2, warm_start=1)
     warm_info = None
     if not args.no_warm:
         warm_info = train_warm_start(eph, system, dev)
-    opts = batch.options(group_steps=2, warm_start=0 if args.no_warm else 1)
 
     def timed(o):
         st = st0.clone()
@@ -279,14 +287,16 @@ def main():
             ms = float(t.item())
         return ms, acc, status.cpu().numpy(), st, wall
 
-    plain = None
+    # the learned warm start, measured beside the plain predictor (the default path)
+    learned = None
     if not args.no_warm:
-        pms, pacc, pstat, pst, _ = timed(plain_opts)
-        pdone = pstat == 0
-        plain = {"value": world * float(np.abs(pop.t_end - pop.t0)[pdone].sum()) * args.steps / (pms / 1e3),
-                 "unit": UNIT, "ms_per_step": pms / args.steps,
-                 "iterations_per_step": pacc["pc_iterations"] / max(pacc["steps_accepted"] + pacc["steps_rejected"], 1),
-                 "force_evals": pacc["force_evals"] // args.steps}
+        lms, lacc, lstat, lst, _ = timed(warm_opts)
+        ldone = lstat == 0
+        learned = {"value": world * float(np.abs(pop.t_end - pop.t0)[ldone].sum()) * args.steps / (lms / 1e3),
+                   "unit": UNIT, "ms_per_step": lms / args.steps,
+                   "iterations_per_step": lacc["pc_iterations"] / max(lacc["steps_accepted"] + lacc["steps_rejected"], 1),
+                   "force_evals": lacc["force_evals"] // args.steps,
+                   "used": lacc["warm_start_used"] // args.steps, "fallback": lacc["warm_start_fallback"] // args.steps}
     clocks = ClockSampler(local)
     clocks.start()
     ms, stats_acc, st_host, st_dev, wall = timed(opts)
@@ -298,8 +308,14 @@ def main():
     bad = int((~done).sum())
     status_counts = {str(k): int(v) for k, v in zip(*np.unique(st_host, return_counts=True))}
     value = world * pdays * args.steps / (ms / 1e3)
-    if plain is not None:
-        plain["max_end_state_difference_au"] = float(np.abs(st_dev.cpu().numpy()[done, :3] - pst.cpu().numpy()[done, :3]).max())
+    if learned is not None:
+        both = done & ldone
+        d = np.abs(st_dev.cpu().numpy()[both, :3] - lst.cpu().numpy()[both, :3]).max(axis=1)
+        learned["ratio_to_plain"] = learned["value"] / (world * pdays * args.steps / (ms / 1e3))
+        learned["end_state_vs_plain_au"] = {"median": float(np.median(d)), "max": float(d.max()),
+                                            "particles_over_1e-9": int((d > 1e-9).sum()),
+                                            "status_mismatches": int((st_host != lstat).sum())}
+        learned.update(warm_info)
     # e2e through the host-array C entry point
     e2e = None
     if rank == 0:
@@ -326,10 +342,10 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .440/SPK ephemeris, seeded population)",
-            "config": {"workload": "batched-65536-mixture-logU30d-10yr", "n_particles": N_PARTICLES,
+            "config": {"workload": WORKLOAD, "n_particles": N_PARTICLES,
                        "particle_days_per_step": pdays, "epsilon": 1e-9, "forces": "0x7F (ASSIST default)",
-                       "warm_start": "plain predictor" if args.no_warm else
-                       "learned (network trained in this run on a separate seeded population)",
+                       "warm_start": "plain predictor (the default; the learned warm start is measured "
+                                     "beside it under learned_warm_start)",
                        "l2": "flushed (256 MB write) between steps", "kernel": "block-cooperative groups (group_steps=2)",
                        "parallelism": "dp%d (independent batches, no collective)" % world},
             "gpu_launches": args.steps, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
@@ -340,8 +356,7 @@ def main():
                       "iterations_per_step": stats_acc["pc_iterations"] / max(stats_acc["steps_accepted"] +
                                                                               stats_acc["steps_rejected"], 1)},
             "unfinished_particles": bad, "status_counts": status_counts, "wall_s_timed_region": wall,
-            "plain_ias15": plain, "warm_start": warm_info and dict(warm_info, used=stats_acc["warm_start_used"] // args.steps,
-                                                                   fallback=stats_acc["warm_start_fallback"] // args.steps)}
+            "learned_warm_start": learned}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -212,6 +212,8 @@ struct assist_gb300_options {
     double dt_floor;        /* a particle whose adaptive step falls below this |dt| (days)
                                stops with ASSIST_GB300_STEP_UNDERFLOW (an impact: any orbit
                                outside a body needs steps > 1e-4 day); 0 disables */
+    int group_order;        /* how groups are formed (group_steps 1, 2): 0 (default) perihelion
+                               distance then length; 1 orbit size, length, then mean anomaly */
 };
 
 /* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */

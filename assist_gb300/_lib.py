@@ -63,6 +63,10 @@ clib.assist_gb300_integrate_batch.restype = c_int
 clib.assist_gb300_integrate_batch_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p,
                                                      c_void_p, c_int, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
 clib.assist_gb300_integrate_batch_device.restype = c_int
+clib.assist_gb300_integrate_batch_dense_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p,
+                                                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                           c_void_p, c_void_p, POINTER(BatchStats)]
+clib.assist_gb300_integrate_batch_dense_device.restype = c_int
 clib.assist_gb300_integrate_batch_device_static.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p,
                                                             c_void_p, c_void_p, c_void_p, c_void_p, POINTER(BatchStats)]
 clib.assist_gb300_integrate_batch_device_static.restype = c_int

@@ -77,6 +77,23 @@ def integrate_batch_device(ephem: Ephem, t0, t_end, state, params=None, var_stat
     return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
 
 
+def integrate_batch_dense_device(ephem: Ephem, t0, t_end, state, out_start, out_t, out_state, params=None,
+                                 status=None, opts: Optional[Options] = None, stream=None):
+    """integrate_batch_device plus dense output: particle i's state at
+    out_t[out_start[i]:out_start[i+1]] (sorted along its integration, within
+    its span) into out_state [*, 6] (torch CUDA tensors; out_start int32)."""
+    o = opts or options()
+    n = state.shape[0]
+    stats = BatchStats()
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_integrate_batch_dense_device(byref(ephem), byref(o), n, _ptr(t0), _ptr(t_end), _ptr(state),
+                                                        _ptr(params), _ptr(out_start), _ptr(out_t), _ptr(out_state),
+                                                        _ptr(status), s, byref(stats))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_integrate_batch_dense_device failed (%d): %s" % (rc, last_error()))
+    return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
+
+
 def integrate_batch_device_static(ephem: Ephem, t0, t_end, state, params=None, status=None,
                                   opts: Optional[Options] = None, stream=None):
     """integrate_batch_device with independent steps and no variational

@@ -586,10 +586,72 @@ struct BatchScratch {
 static std::mutex g_batch_mu;
 static BatchScratch g_batch;
 
+static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                              const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
+                              int n_var, double* d_var_state, int* d_status, void* stream,
+                              struct assist_gb300_batch_stats* stats, const int* d_out_start, const double* d_out_t,
+                              double* d_out_state);
+
 extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e, const struct assist_gb300_options* o,
                                                    int n, const double* d_t0, const double* d_t_end, double* d_state,
                                                    const double* d_params, int n_var, double* d_var_state, int* d_status,
                                                    void* stream, struct assist_gb300_batch_stats* stats) {
+    return ag_integrate_batch(e, o, n, d_t0, d_t_end, d_state, d_params, n_var, d_var_state, d_status, stream, stats,
+                              nullptr, nullptr, nullptr);
+}
+
+extern "C" int assist_gb300_integrate_batch_dense_device(const struct assist_ephem* e,
+                                                         const struct assist_gb300_options* o, int n,
+                                                         const double* d_t0, const double* d_t_end, double* d_state,
+                                                         const double* d_params, const int* d_out_start,
+                                                         const double* d_out_t, double* d_out_state, int* d_status,
+                                                         void* stream, struct assist_gb300_batch_stats* stats) {
+    if (!o || o->group_steps != 2) {
+        ag_set_error("dense output runs in the block-cooperative kernel: group_steps = 2");
+        return ASSIST_ERROR_N;
+    }
+    if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
+    if (!d_out_start || !d_out_t || !d_out_state) { ag_set_error("dense output needs out_start, out_t and out_state"); return ASSIST_ERROR_N; }
+    /* the output times of each particle must lie in its span, in the order of integration */
+    std::vector<int> os((size_t)n + 1);
+    std::vector<double> t0((size_t)n), te((size_t)n);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (ag_cuda_check(cudaMemcpyAsync(os.data(), d_out_start, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s), "read out_start") ||
+        ag_cuda_check(cudaMemcpyAsync(t0.data(), d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
+        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end") ||
+        ag_cuda_check(cudaStreamSynchronize(s), "read dense output layout"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    if (os[0] != 0) { ag_set_error("out_start[0] must be 0"); return ASSIST_ERROR_N; }
+    for (int i = 0; i < n; i++)
+        if (os[(size_t)i + 1] < os[(size_t)i]) { ag_set_error("out_start must be non-decreasing"); return ASSIST_ERROR_N; }
+    std::vector<double> ot((size_t)os[(size_t)n]);
+    if (!ot.empty() &&
+        (ag_cuda_check(cudaMemcpyAsync(ot.data(), d_out_t, sizeof(double) * ot.size(), cudaMemcpyDeviceToHost, s), "read out_t") ||
+         ag_cuda_check(cudaStreamSynchronize(s), "read out_t")))
+        return ASSIST_ERROR_EPHEM_FILE;
+    for (int i = 0; i < n; i++) {
+        const double dir = te[(size_t)i] >= t0[(size_t)i] ? 1.0 : -1.0;
+        double prev = t0[(size_t)i];
+        for (int q = os[(size_t)i]; q < os[(size_t)i + 1]; q++) {
+            const double tq = ot[(size_t)q];
+            if (!(dir * (tq - prev) >= 0.0) || !(dir * (tq - te[(size_t)i]) <= 0.0)) {
+                char msg[200];
+                std::snprintf(msg, sizeof(msg), "particle %d: output time %.17g outside its span or out of order", i, tq);
+                ag_set_error(msg);
+                return ASSIST_ERROR_N;
+            }
+            prev = tq;
+        }
+    }
+    return ag_integrate_batch(e, o, n, d_t0, d_t_end, d_state, d_params, 0, nullptr, d_status, stream, stats,
+                              d_out_start, d_out_t, d_out_state);
+}
+
+static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                              const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
+                              int n_var, double* d_var_state, int* d_status, void* stream,
+                              struct assist_gb300_batch_stats* stats, const int* d_out_start, const double* d_out_t,
+                              double* d_out_state) {
     if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
     if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
     if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
@@ -772,6 +834,7 @@ extern "C" int assist_gb300_integrate_batch_device(const struct assist_ephem* e,
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
     a.dt_floor = o->dt_floor;
     if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
+    a.out_start = d_out_start; a.out_t = d_out_t; a.out_state = d_out_state;
     if (coop && n_var == 0) {
         if (o->warm_start) a.mlp = ag_mlp_device_view();
         float *lx = nullptr, *lt = nullptr;

@@ -398,6 +398,10 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
         }
         bool finish_now = live && (tend == t);
         long long steps = 0;
+        /* dense output cursor (times sorted along the integration) */
+        const bool dense = NV == 0 && A.out_start != nullptr;
+        int on = 0, on_end = 0;
+        if (dense && live) { on = A.out_start[pid]; on_end = A.out_start[pid + 1]; }
         /* warm start per lane: on until its learned starts converge slower than
          * the plain predictor's (every 8th step is a plain probe) */
         bool wl_on = warm;
@@ -409,6 +413,17 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     for (int comp = 0; comp < C; comp++) {
                     if (ag_coop_owner(comp) != wid) continue;
                         const double x1 = W(W_X0, comp) + W(W_XC, comp), v1 = W(W_V0, comp) + W(W_VC, comp);
+                        if (dense && comp < 3) {
+                            /* times left at a completed particle are its t_end: the end
+                             * state; a particle stopped early leaves NaN at the times it
+                             * did not reach */
+                            const bool done_ok = pstat == AG_ST_OK;
+                            const double nan = __longlong_as_double(0x7ff8000000000000LL);
+                            for (int q = on; q < on_end; q++) {
+                                A.out_state[6 * (size_t)q + comp] = done_ok ? x1 : nan;
+                                A.out_state[6 * (size_t)q + 3 + comp] = done_ok ? v1 : nan;
+                            }
+                        }
                         if (comp < 3) {
                             double* s0 = A.state + 6 * (size_t)pid;
                             s0[comp] = x1; s0[3 + comp] = v1;
@@ -715,6 +730,46 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                                 for (int c = 0; c < 3; c++) A.log_t[(size_t)row * AG_MLP_OUT + 3 * k + c] = WS.tgt[k][c][lane];
                         }
                     }
+                }
+            }
+            /* ---- dense output: states at the output times this step covers,
+             * from the step's polynomial (the interpolation of ASSIST's
+             * assist_interpolate, src/assist.c:556-597: s- and sv-coefficients
+             * built by the same recurrences, x from the step-start x, v, a, b) */
+            if (dense && live) {
+                const double tstep_end = (t + tc) + hstep;
+                while (on < on_end && dir * (A.out_t[on] - tstep_end) <= 0.0 && !(last && A.out_t[on] == tend)) {
+                    const double h = ((A.out_t[on] - t) - tc) / hstep;
+                    double s[9], sv[8];
+                    s[0] = hstep * h;
+                    s[1] = s[0] * s[0] / 2.;
+                    s[2] = s[1] * h / 3.;
+                    s[3] = s[2] * h / 2.;
+                    s[4] = 3. * s[3] * h / 5.;
+                    s[5] = 2. * s[4] * h / 3.;
+                    s[6] = 5. * s[5] * h / 7.;
+                    s[7] = 3. * s[6] * h / 4.;
+                    s[8] = 7. * s[7] * h / 9.;
+                    sv[0] = hstep * h;
+                    sv[1] = sv[0] * h / 2.;
+                    sv[2] = 2. * sv[1] * h / 3.;
+                    sv[3] = 3. * sv[2] * h / 4.;
+                    sv[4] = 4. * sv[3] * h / 5.;
+                    sv[5] = 5. * sv[4] * h / 6.;
+                    sv[6] = 6. * sv[5] * h / 7.;
+                    sv[7] = 7. * sv[6] * h / 8.;
+                    if (wid >= 1) {
+                        const int c = wid - 1;
+                        const double b0 = W(W_B + 0, c), b1 = W(W_B + 1, c), b2 = W(W_B + 2, c), b3 = W(W_B + 3, c),
+                                     b4 = W(W_B + 4, c), b5 = W(W_B + 5, c), b6 = W(W_B + 6, c);
+                        const double a0 = W(W_A0, c), v0 = W(W_V0, c);
+                        A.out_state[6 * (size_t)on + c] =
+                            W(W_X0, c) + (s[8] * b6 + s[7] * b5 + s[6] * b4 + s[5] * b3 + s[4] * b2 + s[3] * b1 +
+                                          s[2] * b0 + s[1] * a0 + s[0] * v0);
+                        A.out_state[6 * (size_t)on + 3 + c] = v0 + sv[7] * b6 + sv[6] * b5 + sv[5] * b4 + sv[4] * b3 +
+                                                              sv[3] * b2 + sv[2] * b1 + sv[1] * b0 + sv[0] * a0;
+                    }
+                    on++;
                 }
             }
             /* ---- accept */

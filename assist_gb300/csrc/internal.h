@@ -53,6 +53,11 @@ struct AgBatchArgs {
     float* log_t;                   /* [log_cap][21] their targets */
     int* log_count;                 /* next log row (atomic) */
     int log_cap, log_every;
+    /* dense output (block-cooperative kernel, no variational particles):
+     * particle i's output times out_t[out_start[i] .. out_start[i+1]) */
+    const int* out_start;
+    const double* out_t;
+    double* out_state;              /* [*][6] state at each output time */
 };
 
 /* launchers (kernels_forces.cu, kernels_ias15.cu) */

@@ -265,6 +265,22 @@ int assist_gb300_integrate_batch_device(const struct assist_ephem* ephem, const 
                                         int* d_status, void* stream,
                                         struct assist_gb300_batch_stats* stats);
 
+/* Batched IAS15 with dense output: as assist_gb300_integrate_batch_device
+ * (group_steps = 2, no variational particles) and, on the way, particle i's
+ * state at each of its output times d_out_t[d_out_start[i] ..
+ * d_out_start[i+1]) into d_out_state (6 doubles each), interpolated from the
+ * IAS15 step that contains the time as ASSIST's assist_integrate_or_interpolate
+ * does for one simulation (src/assist.c:556-597, 642-680).  Output times lie
+ * within [t0, t_end] of their particle, in the order of integration
+ * (ASSIST_ERROR_N otherwise); d_out_start has n + 1 entries from 0.  A
+ * particle that stops early (status != 0) leaves NaN at the times it did not
+ * reach. */
+int assist_gb300_integrate_batch_dense_device(const struct assist_ephem* ephem, const struct assist_gb300_options* opt,
+                                              int n, const double* d_t0, const double* d_t_end, double* d_state,
+                                              const double* d_params, const int* d_out_start, const double* d_out_t,
+                                              double* d_out_state, int* d_status, void* stream,
+                                              struct assist_gb300_batch_stats* stats);
+
 /* Batched IAS15 that allocates nothing (no counterpart in the reference).
  * Same integration as assist_gb300_integrate_batch_device with
  * group_steps = 0 and n_var = 0 (independent per-particle steps, identical

@@ -334,8 +334,12 @@ def main():
     kernel_s = stats_acc["kernel_ms"] / 1e3
     peak = batch.fp64_peak_gflops() * 1e9
     achieved = flops / kernel_s
+    # DRAM bytes per launch: 0.578 B per particle-day, from one ncu capture of
+    # this kernel on the 8,192-particle case of this workload (dram__bytes_read
+    # + dram__bytes_write), scaled by the particle-days of a full launch
+    traffic = 0.578 * pdays
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (scaled from ncu)",
             "peak_source": "measured in this run (FP64 FMA chains; MEASURED_PEAKS.json has no FP64 figure)",
             "flops_per_force_eval": per_eval, "op_counts_per_eval": counts}
     cpu = None if args.no_cpu_baseline else cpu_baseline(pl, ast, pop)

@@ -175,3 +175,23 @@ def test_batch_fixed_step_bitwise(synth_files, group_steps):
     ref = O.integrate_batch(pop.t0, pop.t_end, pop.state, epsilon=0.0, dt0=4.0)
     assert (status == 0).all()
     assert np.abs(out - ref).max() <= 1e-15 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("group_steps", [0, 2])
+def test_batch_geocentric_vs_oracle(synth_files, group_steps):
+    """Geocentric frame (ASSIST's `geocentric = 1`, src/forces.c:72-87, 157-172):
+    states relative to the Earth, the Earth's acceleration removed."""
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "neo", 64, seed=23, t0=8000.0, log_len=(20.0, 200.0))
+    earth = np.array(system.body(3, np.array(8000.0))).reshape(2, 3)
+    geo = pop.state.copy()
+    geo[:, :3] -= earth[0]; geo[:, 3:] -= earth[1]
+    o = batch.options(group_steps=group_steps, geocentric=1)
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, geo, opts=o)
+    ref, _, rstat, _ = O.integrate_batch(pop.t0, pop.t_end, geo, geocentric=1, return_all=True)
+    assert np.array_equal(status, rstat)
+    ok = rstat == 0
+    assert np.abs(out[ok, :3] - ref[ok, :3]).max() < 1e-9

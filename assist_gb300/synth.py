@@ -375,6 +375,101 @@ def write_spk_asteroids(path: str, system: SolarSystem, jd_beg: float, jd_end: f
             "ncoef": ncoef}
 
 
+def _spk_comment_records(lines) -> list:
+    """DAF comment records: lines end with NUL, the area with EOT.  A record
+    that ends inside the text ends with one blank so that readers which strip
+    each record's trailing NULs (src/spk.c:49-110) do not join two lines."""
+    recs, cur = [], b""
+    for ln in lines:
+        item = ln.encode("ascii") + b"\0"
+        if len(cur) + len(item) > 998:
+            recs.append(cur + b" ")
+            cur = b""
+        cur += item
+    recs.append(cur + b"\4")
+    return [r + b"\0" * (1024 - len(r)) for r in recs]
+
+
+def write_spk_planets(path: str, system: SolarSystem, jd_beg: float, jd_end: float,
+                      intlen_days: float = 16.0, ncoef: int = 12) -> dict:
+    """Write the planets as a DAF/SPK type-2 file in the layout of the JPL
+    planetary SPK kernels ASSIST reads (src/spk.c, src/assist.c:252-292):
+    planet barycentres 1, 2, 4..9, the Sun 10 and the Earth-Moon barycentre 3
+    about the solar-system barycentre 0; the Moon 301 and the Earth 399 about
+    the Earth-Moon barycentre.  The comment area carries the integration
+    constants and GMs ASSIST parses ("KEY value" lines after "Initial
+    conditions and constants used for integration:", D exponents)."""
+    col = {1: 0, 2: 1, 4: 3, 5: 4, 6: 5, 7: 6, 8: 7, 9: 8}
+    fm = EMRAT / (1.0 + EMRAT)
+    targets = []
+    for code in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10):
+        if code == 10:
+            targets.append((10, 0, lambda t: system.sun(t)[0] * AU_KM))
+        elif code == 3:
+            targets.append((3, 0, lambda t: system.helio_planets(t)[0][..., 2, :] * AU_KM))
+        else:
+            targets.append((code, 0, lambda t, c=col[code]: system.helio_planets(t)[0][..., c, :] * AU_KM))
+    targets.append((301, 3, lambda t: system.moon_geo(t)[0] * fm * AU_KM))
+    targets.append((399, 3, lambda t: -system.moon_geo(t)[0] / (1.0 + EMRAT) * AU_KM))
+    lines = ["Synthetic planetary ephemeris (Keplerian Chebyshev fits).", " ",
+             "Initial conditions and constants used for integration:", " "]
+    d = lambda v: ("%.17E" % v).replace("E", "D")
+    cons = [("AU", AU_KM), ("EMRAT", EMRAT), ("J2E", J2E), ("J3E", J3E), ("J4E", J4E), ("J2SUN", J2SUN),
+            ("RE", RE_KM), ("CLIGHT", CLIGHT), ("ASUN", ASUN_KM), ("GMS", GMS)]
+    cons += [(key, GM_PLANETS[key]) for _, _, key in PLANETS]
+    cons += [("MA%04d" % num, float(gm)) for num, gm in zip(ASTEROID_NUMBERS, system.gm_asteroids)]
+    lines += ["%-8s %s" % (k, d(v)) for k, v in cons]
+    crecs = _spk_comment_records(lines)
+    fward = 2 + len(crecs)
+    addr = (fward + 1) * 128 + 1
+    summaries, segments = [], []
+    for code, cen, f in targets:
+        # shorter records for the Moon and the Earth about the Earth-Moon
+        # barycentre and for Mercury, as the JPL kernels have
+        ilen_d = intlen_days / 4.0 if code in (301, 399) else (intlen_days / 2.0 if code == 1 else intlen_days)
+        n_int = int(math.ceil((jd_end - jd_beg) / ilen_d - 1e-12))
+        init = (jd_beg - JD_J2000) * DAY_S
+        intlen = ilen_d * DAY_S
+        rsize = 2 + 3 * ncoef
+        seg_len = n_int * rsize + 4
+        ta = jd_beg - JD_J2000 + ilen_d * np.arange(n_int)
+        c = cheb_fit(f, ta, ta + ilen_d, ncoef)
+        recs = np.zeros((n_int, rsize))
+        recs[:, 0] = init + intlen * (np.arange(n_int) + 0.5)
+        recs[:, 1] = 0.5 * intlen
+        recs[:, 2:] = c.reshape(n_int, 3 * ncoef)
+        seg = np.concatenate([recs.ravel(), [init, intlen, float(rsize), float(n_int)]])
+        one, two = addr, addr + seg_len - 1
+        summaries.append((init, init + n_int * intlen, code, cen, 1, 2, one, two))
+        segments.append(seg)
+        addr = two + 1
+    filerec = bytearray(1024)
+    filerec[0:8] = b"DAF/SPK "
+    filerec[8:16] = struct.pack("<ii", 2, 6)
+    name = b"synthetic planetary SPK (Keplerian Chebyshev fit)"
+    filerec[16:76] = name + b" " * (60 - len(name))
+    filerec[76:88] = struct.pack("<iii", fward, fward, addr)
+    filerec[88:96] = b"LTL-IEEE"
+    sumrec = bytearray(1024)
+    sumrec[0:24] = struct.pack("<ddd", 0.0, 0.0, float(len(summaries)))
+    for i, s_ in enumerate(summaries):
+        sumrec[24 + 40 * i: 24 + 40 * (i + 1)] = struct.pack("<dd6i", *s_)
+    namerec = bytearray(b" " * 1024)
+    for i, s_ in enumerate(summaries):
+        nm = b"BODY %d" % s_[2]
+        namerec[40 * i:40 * i + len(nm)] = nm
+    blob = np.concatenate(segments).astype("<f8").tobytes()
+    pad = (-len(blob)) % 1024
+    with open(path, "wb") as f_:
+        f_.write(bytes(filerec))
+        for r in crecs:
+            f_.write(r)
+        f_.write(bytes(sumrec))
+        f_.write(bytes(namerec))
+        f_.write(blob + b"\0" * pad)
+    return {"jd_beg": jd_beg, "jd_end": jd_end, "ncoef": ncoef}
+
+
 def write_ephemeris(dirpath: str, seed: int = 20240611, t_beg: float = 7800.0, t_end: float = 12000.0):
     """Write planets (.440 layout) + asteroids (SPK) covering [t_beg, t_end]
     (days relative to JD 2451545.0).  Returns (planets_path, asteroids_path, system)."""
@@ -388,6 +483,17 @@ def write_ephemeris(dirpath: str, seed: int = 20240611, t_beg: float = 7800.0, t
     write_ascii_ephem(pl, system, jd0, n_rec, inc)
     write_spk_asteroids(ast, system, jd0 - inc, jd0 + (n_rec + 1) * inc)
     return pl, ast, system
+
+
+def write_planets_spk(dirpath: str, system: SolarSystem, seed: int, t_beg: float, t_end: float) -> str:
+    """The same planets as an SPK file (16-day records) covering [t_beg, t_end]."""
+    import os
+    inc = 32.0
+    jd0 = JD_J2000 + inc * math.floor(t_beg / inc)
+    n_rec = int(math.ceil((JD_J2000 + t_end - jd0) / inc))
+    path = os.path.join(dirpath, "synthetic_%d_planets.bsp" % seed)
+    write_spk_planets(path, system, jd0, jd0 + n_rec * inc)
+    return path
 
 
 # ---------------------------------------------------------------------------

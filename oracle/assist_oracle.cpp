@@ -10,6 +10,11 @@
  *   - planet evaluation incl. Earth/Moon split  src/ascii_ephem.c:275-384
  *   - DAF/SPK type-2 loader                      src/spk.c:267-402
  *   - asteroid (position-only) evaluation        src/spk.c:405-481
+ *   - planets from an SPK file: comment constants and masses, target
+ *     evaluation with T/S/U recurrences, Earth/Moon about the Earth-Moon
+ *     barycentre                                 src/spk.c:49-110, 137-200,
+ *                                                492-693, 695-800;
+ *                                                src/assist.c:252-292
  *   - body dispatch incl. asteroid+Sun offset    src/forces.c:175-263
  *   - force dispatcher and term order            src/forces.c:49-173
  *   - direct gravity (+ variational)             src/forces.c:266-433
@@ -188,7 +193,7 @@ static Spk* spk_load(const char* path) {
             for (auto& x : s->targets) if (x.code == tar) { t = &x; break; }
             if (!t) {
                 SpkTarget nt;
-                nt.code = tar; nt.cen = cen; nt.mass = 0;
+                nt.code = tar; nt.cen = cen; nt.mass = 0; nt.end = 0;
                 nt.beg = 2451545.0 + sbeg / 86400.0;
                 nt.res = (2451545.0 + send / 86400.0) - nt.beg;
                 s->targets.push_back(nt);
@@ -208,12 +213,121 @@ struct Ephem {
     double jd_ref = 2451545.0;
     Ascii* pl = nullptr;
     Spk* ast = nullptr;
+    Spk* pls = nullptr;                 /* planets from an SPK file (else pl) */
+    int tgt[NPL] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+    int emb = -1;
     double AU, EMRAT, J2E, J3E, J4E, J2SUN, RE, CLIGHT, ASUN, Re_eq, Rs_eq, c_AU_per_day, c_squared, over_c_squared;
     int n_ast() const { return ast ? (int)ast->targets.size() : 0; }
 };
 
-/* src/assist.c:252-348 for the .440 branch; SPK planets are not restated. */
+/* DAF comment area: records 2 .. fward-1, trailing NUL/EOT bytes of each
+ * record dropped, NUL ends a line (src/spk.c:49-110). */
+static std::string spk_comments(const std::vector<unsigned char>& b) {
+    std::string out;
+    if (b.size() < 1024) return out;
+    const int fward = rd<int32_t>(b, 76);
+    for (int r = 0; r < fward - 2; r++) {
+        size_t o = (size_t)(1 + r) * 1024;
+        if (o + 1024 > b.size()) break;
+        int len = 1024;
+        while (len > 0 && (b[o + len - 1] == 0 || b[o + len - 1] == 4)) len--;
+        for (int k = 0; k < len; k++) out.push_back(b[o + k] == 0 ? '\n' : (char)b[o + k]);
+    }
+    return out;
+}
+
+/* "KEY value" lines after "Initial conditions and constants used for
+ * integration:", D exponents read as E (src/spk.c:695-760). */
+struct SpkConst { double AU = 0, EMRAT = 0, J2E = 0, J3E = 0, J4E = 0, J2SUN = 0, RE = 0, CLIGHT = 0, ASUN = 0;
+                  std::vector<std::pair<std::string, double>> masses; };
+static SpkConst spk_constants(const std::string& c) {
+    SpkConst k;
+    bool in = false;
+    size_t pos = 0;
+    while (pos < c.size()) {
+        size_t e = c.find('\n', pos);
+        if (e == std::string::npos) e = c.size();
+        std::string line = c.substr(pos, e - pos);
+        pos = e + 1;
+        if (line.empty()) continue;
+        if (line.find("Initial conditions and constants used for integration:") != std::string::npos) in = true;
+        if (!in) continue;
+        for (auto& ch : line) if (ch == 'D' || ch == 'd') ch = 'E';
+        char key[64], val[64];
+        if (std::sscanf(line.c_str(), "%63s %63s", key, val) != 2) continue;
+        const double v = std::strtod(val, nullptr);
+        std::string K(key);
+        if (K == "cau" || K == "AU") k.AU = v;
+        else if (K == "EMRAT") k.EMRAT = v;
+        else if (K == "J2E") k.J2E = v;
+        else if (K == "J3E") k.J3E = v;
+        else if (K == "J4E") k.J4E = v;
+        else if (K == "J2SUN") k.J2SUN = v;
+        else if (K == "RE") k.RE = v;
+        else if (K == "CLIGHT") k.CLIGHT = v;
+        else if (K == "ASUN") k.ASUN = v;
+        else if (K.compare(0, 2, "GM") == 0 || K.compare(0, 2, "MA") == 0) k.masses.push_back({K, v});
+    }
+    return k;
+}
+
+/* Masses of SPK targets from the parsed GMs (src/spk.c:137-200): planets by
+ * name, Earth and Moon split from GMB by EMRAT, asteroids as MAnnnn. */
+static void spk_join_masses(Spk* s, const SpkConst& k) {
+    if (!s) return;
+    static const struct { const char* name; int code; } pc[] = {
+        {"GMS", 10}, {"GM1", 1}, {"GM2", 2}, {"GMB", 399}, {"GMB", 3}, {"GMB", 301}, {"GM4", 4},
+        {"GM5", 5}, {"GM6", 6}, {"GM7", 7}, {"GM8", 8}, {"GM9", 9}};
+    for (auto& t : s->targets) {
+        if (t.mass != 0) continue;
+        char label[64] = {0};
+        for (auto& q : pc) if (t.code == q.code) { std::snprintf(label, sizeof(label), "%s", q.name); break; }
+        if (!label[0]) std::snprintf(label, sizeof(label), "MA%04d", t.code - 2000000);
+        for (auto& m : k.masses) {
+            if (m.first != label) continue;
+            if (t.code == 399) t.mass = m.second * (k.EMRAT / (1. + k.EMRAT));
+            else if (t.code == 301) t.mass = m.second * (1. / (1. + k.EMRAT));
+            else t.mass = m.second;
+            break;
+        }
+    }
+}
+
+/* src/assist.c:252-292: planets from an SPK file. */
+static Ephem* ephem_load_spk(const char* planets, const char* asteroids) {
+    std::vector<unsigned char> b;
+    if (!read_all(planets, b)) return nullptr;
+    Spk* ps = spk_load(planets);
+    if (!ps) return nullptr;
+    Ephem* e = new Ephem();
+    e->pls = ps;
+    static const int naif[NPL] = {10, 1, 2, 399, 301, 4, 5, 6, 7, 8, 9};
+    for (int k = 0; k < NPL; k++)
+        for (int i = 0; i < (int)ps->targets.size(); i++)
+            if (ps->targets[(size_t)i].code == naif[k]) { e->tgt[k] = i; break; }
+    for (int i = 0; i < (int)ps->targets.size(); i++)
+        if (ps->targets[(size_t)i].code == 3) { e->emb = i; break; }
+    e->ast = asteroids ? spk_load(asteroids) : nullptr;
+    const SpkConst k = spk_constants(spk_comments(b));
+    e->AU = k.AU; e->EMRAT = k.EMRAT; e->J2E = k.J2E; e->J3E = k.J3E; e->J4E = k.J4E; e->J2SUN = k.J2SUN;
+    e->RE = k.RE; e->CLIGHT = k.CLIGHT; e->ASUN = k.ASUN;
+    e->Re_eq = e->RE / e->AU;
+    e->Rs_eq = e->ASUN / e->AU;
+    e->c_AU_per_day = (e->CLIGHT / e->AU) * 86400;
+    e->c_squared = e->c_AU_per_day * e->c_AU_per_day;
+    e->over_c_squared = 1.0 / e->c_squared;
+    spk_join_masses(e->pls, k);
+    spk_join_masses(e->ast, k);
+    return e;
+}
+
+/* src/assist.c:252-348 for the .440 branch (and the SPK branch above). */
 static Ephem* ephem_load(const char* planets, const char* asteroids) {
+    {
+        std::vector<unsigned char> b;
+        if (read_all(planets, b) && b.size() >= 8 && std::memcmp(b.data(), "DAF/SPK", 7) == 0)
+            return ephem_load_spk(planets, asteroids);
+    }
     Ascii* a = ascii_load(planets);
     if (!a) return nullptr;
     Ephem* e = new Ephem();
@@ -399,16 +513,90 @@ static int spk_position(const Ephem& e, T t, int m, T* gm, T* pos) {
     return OK;
 }
 
+/* Position, velocity, acceleration sums of one SPK target (km, km/s,
+ * km/s^2) with the T, S, U recurrences of src/spk.c:492-548. */
+template <class T>
+static void spk_target_pos(const Spk& s, const SpkTarget& tg, const Ephem& e, T t, T* u, T* v, T* w) {
+    int n = (int)to_double((T(e.jd_ref) + t - tg.beg) / tg.res);
+    if (n >= (int)tg.two.size()) n = (int)tg.two.size() - 1;    // at the very end (the reference reads past)
+    const double* dir = s.data.data() + tg.two[n] - 1;
+    const int R = (int)dir[-1];
+    const int P = (R - 2) / 3;
+    int b = (int)to_double(((T(e.jd_ref) - (2451545.0 + dir[-3] / 86400.0)) + t) / (dir[-2] / 86400.0));
+    const int nrec = (int)dir[0];
+    if (b >= nrec) b = nrec - 1;
+    const double* val = s.data.data() + (tg.one[n] - 1) + (size_t)b * R;
+    T z = ((T(e.jd_ref) - (2451545.0 + val[0] / 86400.0)) + t) / (val[1] / 86400.0);
+    const double c = 1.0 / val[1];
+    T Tp[32], Sp[32], Up[32];
+    Tp[0] = 1.0; Tp[1] = z;
+    Sp[0] = 0.0; Sp[1] = 1.0;
+    Up[0] = 0.0; Up[1] = 0.0; Up[2] = 4.0;
+    for (int p = 2; p < P; p++) {
+        Tp[p] = 2.0 * z * Tp[p - 1] - Tp[p - 2];
+        Sp[p] = 2.0 * z * Sp[p - 1] + 2.0 * Tp[p - 1] - Sp[p - 2];
+    }
+    for (int p = 3; p < P; p++) Up[p] = 2.0 * z * Up[p - 1] + 4.0 * Sp[p - 1] - Up[p - 2];
+    for (int k = 0; k < 3; k++) {
+        const int b0 = 2 + k * P;
+        T su = 0.0, sv = 0.0, sw = 0.0;
+        for (int p = 0; p < P; p++) {
+            const double coeff = val[b0 + p];
+            su += coeff * Tp[p];
+            sv += coeff * Sp[p] * c;
+            sw += coeff * Up[p] * c * c;
+        }
+        u[k] = su; v[k] = sv; w[k] = sw;
+    }
+}
+
+/* Planet state from an SPK planets file, src/spk.c:550-693: the target of
+ * the ASSIST body (Earth 399 and Moon 301 plus the Earth-Moon barycentre),
+ * in AU and days.  out: GM, x,y,z, vx,vy,vz, ax,ay,az. */
+template <class T>
+static int spk_body(const Ephem& e, T t, int body, T* out) {
+    if (body < 0 || body >= NPL || e.tgt[body] < 0) return ERR_NEPHEM;
+    const Spk& s = *e.pls;
+    const SpkTarget& tg = s.targets[(size_t)e.tgt[body]];
+    double jd = to_double(T(e.jd_ref) + t);
+    if (jd < tg.beg || jd > tg.end) return ERR_COVERAGE;
+    out[0] = tg.mass;
+    T u[3], v[3], w[3];
+    spk_target_pos(s, tg, e, t, u, v, w);
+    if (body == B_EAR || body == B_MOO) {
+        T eu[3], ev[3], ew[3];
+        spk_target_pos(s, s.targets[(size_t)e.emb], e, t, eu, ev, ew);
+        for (int k = 0; k < 3; k++) { u[k] += eu[k]; v[k] += ev[k]; w[k] += ew[k]; }
+    }
+    const double au = e.AU, spd = 86400.;
+    for (int k = 0; k < 3; k++) {
+        out[1 + k] = u[k] / au;
+        out[4 + k] = v[k] / (au / spd);
+        out[7 + k] = w[k] / (au / (spd * spd));
+    }
+    return OK;
+}
+
+/* Planet i from whichever planets file is loaded. */
+template <class T>
+static int planet_body(const Ephem& e, T t, int body, T* out) {
+    return e.pls ? spk_body(e, t, body, out) : ascii_body(e, t, body, out);
+}
+template <class T>
+static int planet_body_need(const Ephem& e, T t, int body, T* out, bool vel, bool acc) {
+    return e.pls ? spk_body(e, t, body, out) : ascii_body_need(e, t, body, out, vel, acc);
+}
+
 /* Body i at time t, src/forces.c:175-263 (no cache: the reference's cache
  * returns bit-identical values, unit_tests/ephem_cache). */
 template <class T>
 static int body_state(const Ephem& e, int i, T t, T* out) {
-    if (i < NPL) return ascii_body(e, t, i, out);
+    if (i < NPL) return planet_body(e, t, i, out);
     T gm, p[3];
     int f = spk_position(e, t, i - NPL, &gm, p);
     if (f != OK) return f;
     T sun[10];
-    f = ascii_body(e, t, B_SUN, sun);
+    f = planet_body(e, t, B_SUN, sun);
     if (f != OK) return f;
     out[0] = gm;
     out[1] = p[0] + sun[1]; out[2] = p[1] + sun[2]; out[3] = p[2] + sun[3];
@@ -444,7 +632,7 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
      * only the derivatives the force model reads, gives identical values and
      * an operation count without the reference's redundant work. */
     for (int i = 0; i < NPL; i++) {
-        int f = ascii_body_need(e, t, i, &B[(size_t)i * 10], need_velocity(o, i), o.geocentric == 1 && i == B_EAR);
+        int f = planet_body_need(e, t, i, &B[(size_t)i * 10], need_velocity(o, i), o.geocentric == 1 && i == B_EAR);
         if (f != OK) return f;
     }
     for (int i = NPL; i < nb; i++) {
@@ -1189,7 +1377,7 @@ void* orc_ephem_load(const char* planets, const char* asteroids) { return ephem_
 void orc_ephem_free(void* h) {
     Ephem* e = (Ephem*)h;
     if (!e) return;
-    delete e->pl; delete e->ast; delete e;
+    delete e->pl; delete e->ast; delete e->pls; delete e;
 }
 int orc_n_bodies(void* h) { return NPL + ((Ephem*)h)->n_ast(); }
 int orc_body(void* h, int i, double t, double* out) {
@@ -1199,7 +1387,12 @@ int orc_body(void* h, int i, double t, double* out) {
 }
 void orc_time_bounds(void* h, double* tb, double* te) {
     Ephem* e = (Ephem*)h;
-    double b = e->pl->beg, en = e->pl->end;
+    double b = -INFINITY, en = INFINITY;
+    if (e->pls) {
+        for (auto& t : e->pls->targets) { if (t.beg > b) b = t.beg; if (t.end < en) en = t.end; }
+    } else {
+        b = e->pl->beg; en = e->pl->end;
+    }
     if (e->ast) for (auto& t : e->ast->targets) { if (t.beg > b) b = t.beg; if (t.end < en) en = t.end; }
     *tb = b - e->jd_ref; *te = en - e->jd_ref;
 }

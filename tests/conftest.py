@@ -28,14 +28,21 @@ def pytest_configure(config):
         mod.build_library()
 
 
-@pytest.fixture(scope="session")
-def golden():
-    return dict(np.load(os.path.join(GOLDEN, "golden.npz")))
+@pytest.fixture(scope="session", params=["440", "bsp"])
+def planets_format(request):
+    """The golden planets as a .440 file and as an SPK file (same orbits)."""
+    return request.param
 
 
 @pytest.fixture(scope="session")
-def golden_paths():
-    return os.path.join(GOLDEN, "golden_planets.440"), os.path.join(GOLDEN, "golden_asteroids.bsp")
+def golden(planets_format):
+    return dict(np.load(os.path.join(GOLDEN, "golden.npz" if planets_format == "440" else "golden_spk.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_paths(planets_format):
+    return (os.path.join(GOLDEN, "golden_planets." + planets_format),
+            os.path.join(GOLDEN, "golden_asteroids.bsp"))
 
 
 @pytest.fixture(scope="session")

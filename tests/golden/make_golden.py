@@ -6,8 +6,12 @@ Run in a container where the ASSIST sources are present (default
     sh oracle/build_ref.sh && python tests/golden/make_golden.py
 
 Writes
-  golden_planets.440, golden_asteroids.bsp  -- a small synthetic ephemeris
-  golden.npz                                -- reference outputs on it:
+  golden_planets.440, golden_planets.bsp,
+  golden_asteroids.bsp                      -- a small synthetic ephemeris
+                                               (the same planets as a .440
+                                               file and as an SPK file)
+  golden.npz, golden_spk.npz                -- reference outputs on it with
+                                               each planets file:
       body states, accelerations for several force configurations
       (variational particles, non-grav parameters, geocentric, EIH sources),
       and IAS15 end states with the reference's forces.
@@ -68,13 +72,25 @@ def detection_samples():
 
 def main():
     pl = os.path.join(HERE, "golden_planets.440")
+    plb = os.path.join(HERE, "golden_planets.bsp")
     ast = os.path.join(HERE, "golden_asteroids.bsp")
     system = synth.SolarSystem(4242)
     synth.write_ascii_ephem(pl, system, synth.JD_J2000 + 32.0 * 249, 9)        # t in [7968, 8256]
+    synth.write_spk_planets(plb, system, synth.JD_J2000 + 32.0 * 249, synth.JD_J2000 + 32.0 * 258)
     synth.write_spk_asteroids(ast, system, synth.JD_J2000 + 32.0 * 248, synth.JD_J2000 + 32.0 * 259)
     R = ref_lib()
-    e = R.refh_ephem_create(pl.encode(), ast.encode())
-    assert e, "reference could not load the golden ephemeris"
+    for planets, out in ((pl, "golden.npz"), (plb, "golden_spk.npz")):
+        e = R.refh_ephem_create(planets.encode(), ast.encode())
+        assert e, "reference could not load the golden ephemeris " + planets
+        g = reference_outputs(R, e, system)
+        np.savez_compressed(os.path.join(HERE, out), **g)
+        print("wrote", out, sorted(g))
+    np.savez_compressed(os.path.join(HERE, "detection.npz"), **detection_samples())
+
+
+def reference_outputs(R, e, system):
+    """Body states, accelerations of the force cases and IAS15 end states of
+    the reference on one ephemeris (planets file + asteroids file)."""
     g = {}
     # body states
     times = np.linspace(7970.0, 8250.0, 29)
@@ -140,9 +156,7 @@ def main():
     g["int_t1"] = np.array(8200.0)
     g["int_state0"] = int_state
     g["int_end"] = np.array(integ)
-    np.savez_compressed(os.path.join(HERE, "golden.npz"), **g)
-    np.savez_compressed(os.path.join(HERE, "detection.npz"), **detection_samples())
-    print("wrote golden fixtures:", sorted(g))
+    return g
 
 
 if __name__ == "__main__":

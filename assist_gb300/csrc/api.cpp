@@ -700,7 +700,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         /* groups share t0 and direction; within them particles of similar
          * orbital timescale (perihelion distance q^1.5, quarter-octave bins)
          * and similar length sit together; groups are queued longest first */
-        const double gm = e->ascii_planets ? ag_sun_gm(e) : 2.9591220828411951e-04;
+        const double gm = (e->ascii_planets || e->spk_planets) ? ag_sun_gm(e) : 2.9591220828411951e-04;
         std::vector<int> bucket((size_t)n);
         std::vector<double> qper((size_t)n);
         for (int i = 0; i < n; i++) {

@@ -65,6 +65,17 @@ struct DevEphem {
     int ast_nseg[AG_MAX_AST], ast_seg0[AG_MAX_AST];
     const struct AgSpkSeg* segs; /* per segment, see AgSpkSeg */
     const double4* rec_meta;     /* per SPK record: (MID as JD, RADIUS/86400, 86400/RADIUS, 0) */
+    /* planets from an SPK file (pl_spk = 1) instead of the .440 record:
+     * segments of the eleven bodies' targets (Sun 10, Mercury 1, Venus 2,
+     * Earth 399, Moon 301, Mars 4 .. Pluto 9) and, in slot 11, the Earth-Moon
+     * barycentre 3 that Earth and Moon are stored about */
+    int pl_spk;
+    const double* pspk;          /* the whole planets SPK file as doubles */
+    const struct AgSpkSeg* psegs;
+    const double4* pmeta;
+    int ps_seg0[AG_NPL + 1], ps_nseg[AG_NPL + 1];
+    double ps_beg[AG_NPL + 1], ps_end[AG_NPL + 1], ps_res[AG_NPL + 1];
+    double au_km;                /* the file's AU (km) */
     /* constants (ASSIST src/assist.c:296-309) */
     double J2E, J3E, J4E, J2SUN, Re_eq, Rs_eq, c_squared, over_c_squared;
     /* device copy of this view: kernels read the ephemeris through it (a
@@ -295,7 +306,10 @@ __device__ __forceinline__ void ag_column_pva_exact(const DevEphem& E, const dou
     }
 }
 
+__device__ inline int ag_spk_planet(const DevEphem& E, int body, double t, double* out);
+
 __device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out) {
+    if (E.pl_spk) return ag_spk_planet(E, body, t, out);
     const double* rec;
     double tf;
     out[0] = E.gm[body];
@@ -320,6 +334,71 @@ __device__ inline int ag_planet_full(const DevEphem& E, int body, double t, doub
         out[1 + k] = __ddiv_rn(u[k], E.pl_cau);
         out[4 + k] = __ddiv_rn(v[k], E.cau_per_day);
         out[7 + k] = __ddiv_rn(w[k], acc_div);
+    }
+    return AG_OK;
+}
+
+/* Position, velocity and acceleration sums (km, km/s, km/s^2) of planets-SPK
+ * slot `slot` at time t, in the operations and order of
+ * assist_spk_target_pos (src/spk.c:492-548): segment n from the target's
+ * begin epoch and step, record b from the segment directory, z from the
+ * record's MID and RADIUS, T/S/U recurrences, c = 1/RADIUS[s]. */
+__device__ inline void ag_spk_target_pva(const DevEphem& E, int slot, double t, double* u, double* v, double* w) {
+    int n = (int)__ddiv_rn(__dsub_rn(__dadd_rn(E.jd_ref, t), E.ps_beg[slot]), E.ps_res[slot]);
+    if (n >= E.ps_nseg[slot]) n = E.ps_nseg[slot] - 1;
+    if (n < 0) n = 0;
+    const AgSpkSeg sg = E.psegs[E.ps_seg0[slot] + n];
+    int b = (int)(__ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, sg.init_jd), t), sg.intlen_days));
+    if (b >= sg.nrec) b = sg.nrec - 1;
+    if (b < 0) b = 0;
+    const double4 meta = E.pmeta[sg.meta_off + b];
+    const double* val = E.pspk + sg.data_off + (size_t)b * sg.R;
+    const int P = sg.P;
+    const double z = __ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, meta.x), t), meta.y);
+    const double c = __ddiv_rn(1.0, val[1]);
+    const double two_z = __dmul_rn(2.0, z);
+    double T[AG_MAX_SPK_P], S[AG_MAX_SPK_P], U[AG_MAX_SPK_P];
+    T[0] = 1.0; T[1] = z; S[0] = 0.0; S[1] = 1.0; U[0] = 0.0; U[1] = 0.0; U[2] = 4.0;
+    for (int p = 2; p < P; p++) {
+        T[p] = __dsub_rn(__dmul_rn(two_z, T[p - 1]), T[p - 2]);
+        S[p] = __dsub_rn(__dadd_rn(__dmul_rn(two_z, S[p - 1]), __dmul_rn(2.0, T[p - 1])), S[p - 2]);
+    }
+    for (int p = 3; p < P; p++)
+        U[p] = __dsub_rn(__dadd_rn(__dmul_rn(two_z, U[p - 1]), __dmul_rn(4.0, S[p - 1])), U[p - 2]);
+    for (int k = 0; k < 3; k++) {
+        const double* cf = val + 2 + k * P;
+        double su = 0.0, sv = 0.0, sw = 0.0;
+        for (int p = 0; p < P; p++) {
+            su = __dadd_rn(su, __dmul_rn(cf[p], T[p]));
+            sv = __dadd_rn(sv, __dmul_rn(__dmul_rn(cf[p], S[p]), c));
+            sw = __dadd_rn(sw, __dmul_rn(__dmul_rn(__dmul_rn(cf[p], U[p]), c), c));
+        }
+        u[k] = su; v[k] = sv; w[k] = sw;
+    }
+}
+
+/* Planet `body` from the planets SPK file as ASSIST's
+ * assist_spk_calc_planets_from_target forms it (src/spk.c:550-608): Earth
+ * and Moon plus the Earth-Moon barycentre, then km -> AU, AU/day, AU/day^2.
+ * out: GM, x,y,z, vx,vy,vz, ax,ay,az. */
+__device__ inline int ag_spk_planet(const DevEphem& E, int body, double t, double* out) {
+    const double jd = E.jd_ref + t;
+    out[0] = E.gm[body];
+    if (E.ps_nseg[body] <= 0) return AG_ERR_NEPHEM;
+    if (jd < E.ps_beg[body] || jd > E.ps_end[body]) return AG_ERR_COVERAGE;
+    double u[3], v[3], w[3];
+    ag_spk_target_pva(E, body, t, u, v, w);
+    if (body == AG_EAR || body == AG_MOO) {
+        double eu[3], ev[3], ew[3];
+        ag_spk_target_pva(E, AG_NPL, t, eu, ev, ew);
+        for (int k = 0; k < 3; k++) { u[k] = __dadd_rn(u[k], eu[k]); v[k] = __dadd_rn(v[k], ev[k]); w[k] = __dadd_rn(w[k], ew[k]); }
+    }
+    const double vdiv = __ddiv_rn(E.au_km, 86400.);
+    const double adiv = __ddiv_rn(E.au_km, __dmul_rn(86400., 86400.));
+    for (int k = 0; k < 3; k++) {
+        out[1 + k] = __ddiv_rn(u[k], E.au_km);
+        out[4 + k] = __ddiv_rn(v[k], vdiv);
+        out[7 + k] = __ddiv_rn(w[k], adiv);
     }
     return AG_OK;
 }

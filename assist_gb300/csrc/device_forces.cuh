@@ -80,6 +80,19 @@ __device__ __forceinline__ void ag_eih_source(const DevEphem& E, const PlanetSta
  * n_vel bodies; Earth's acceleration when geocentric) at time t with the
  * exact arithmetic of the reference. */
 __device__ __forceinline__ int ag_planets_at(const DevEphem& E, double t, int n_vel, bool earth_acc, PlanetState& P) {
+    if (E.pl_spk) {
+        /* planets SPK: every body's full state (src/spk.c:550-608) */
+#pragma unroll 1
+        for (int b = 0; b < AG_NPL; b++) {
+            double o[10];
+            const int st = ag_spk_planet(E, b, t, o);
+            if (st != AG_OK) return st;
+            P.x[b] = o[1]; P.y[b] = o[2]; P.z[b] = o[3];
+            P.vx[b] = o[4]; P.vy[b] = o[5]; P.vz[b] = o[6];
+            if (b == AG_EAR && earth_acc) { P.ex_a[0] = o[7]; P.ex_a[1] = o[8]; P.ex_a[2] = o[9]; }
+        }
+        return AG_OK;
+    }
     const double* rec;
     double tf;
     int st = ag_planet_record(E, t, &rec, &tf);

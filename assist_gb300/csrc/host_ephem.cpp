@@ -11,10 +11,13 @@
  *     src/ascii_ephem.c:105-252 (EMRAT split of GMB into Earth and Moon);
  *   - SPK summaries collected per target, segment directories, and the
  *     asteroid GMs from the .440 "MAnnnn" constants (src/assist.c:311-333).
+ *   - planets from an SPK (.bsp) file: the constants and GMs of the
+ *     comment area (src/spk.c:49-110, 695-800), masses joined to targets
+ *     by name with the Earth/Moon split of GMB (src/spk.c:137-200), target
+ *     indices of the eleven bodies and of the Earth-Moon barycentre
+ *     (src/assist.c:252-292).
  * The parsed files are copied to device memory once; the kernels read the
- * same words ASSIST reads through its mmap.  Planets from an SPK (.bsp)
- * file are recognised but not evaluated by this library: the planets file
- * must be in the .440/.441 layout.
+ * same words ASSIST reads through its mmap.
  */
 #include <cmath>
 #include <cstdio>
@@ -64,9 +67,12 @@ struct spk_s {
     std::vector<AgSpkSeg> segs;
     std::vector<double4> meta;
     std::vector<int> seg0;
+    std::string comments;            /* comment area, NUL -> newline */
     double* d_data = nullptr;
     AgSpkSeg* d_segs = nullptr;
     double4* d_meta = nullptr;
+    DevEphem* d_view = nullptr;      /* planets files: device copy of the last view */
+    DevEphem h_view;
 };
 
 static bool read_file(const char* path, std::vector<unsigned char>& out) {
@@ -243,6 +249,15 @@ static spk_s* spk_load(const char* path) {
     }
     s->data.resize(b.size() / 8);
     std::memcpy(s->data.data(), b.data(), s->data.size() * 8);
+    /* comment records 2 .. fward-1: trailing NUL/EOT bytes of each record
+     * dropped, NUL ends a line (src/spk.c:49-110) */
+    for (int r = 0; r < fward - 2; r++) {
+        const size_t o = (size_t)(1 + r) * 1024;
+        if (o + 1024 > b.size()) break;
+        int len = 1024;
+        while (len > 0 && (b[o + len - 1] == 0 || b[o + len - 1] == 4)) len--;
+        for (int k = 0; k < len; k++) s->comments.push_back(b[o + k] == 0 ? '\n' : (char)b[o + k]);
+    }
     /* segment table with the per-call Julian-date conversions done once */
     for (auto& t : s->targets) {
         s->seg0.push_back((int)s->segs.size());
@@ -295,16 +310,107 @@ static void spk_free(spk_s* s) {
     if (s->d_data) cudaFree(s->d_data);
     if (s->d_segs) cudaFree(s->d_segs);
     if (s->d_meta) cudaFree(s->d_meta);
+    if (s->d_view) cudaFree(s->d_view);
     delete s;
 }
 
+/* Constants and GMs of a planets SPK file: "KEY value" lines after "Initial
+ * conditions and constants used for integration:", D exponents read as E
+ * (src/spk.c:695-760). */
+struct spk_constants {
+    double AU = 0, EMRAT = 0, J2E = 0, J3E = 0, J4E = 0, J2SUN = 0, RE = 0, CLIGHT = 0, ASUN = 0;
+    std::vector<std::pair<std::string, double>> masses;
+};
+static spk_constants spk_parse_constants(const std::string& c) {
+    spk_constants k;
+    bool in = false;
+    size_t pos = 0;
+    while (pos < c.size()) {
+        size_t e = c.find('\n', pos);
+        if (e == std::string::npos) e = c.size();
+        std::string line = c.substr(pos, e - pos);
+        pos = e + 1;
+        if (line.empty()) continue;
+        if (line.find("Initial conditions and constants used for integration:") != std::string::npos) in = true;
+        if (!in) continue;
+        for (auto& ch : line) if (ch == 'D' || ch == 'd') ch = 'E';
+        char key[64], val[64];
+        if (std::sscanf(line.c_str(), "%63s %63s", key, val) != 2) continue;
+        const double v = std::strtod(val, nullptr);
+        const std::string K(key);
+        if (K == "cau" || K == "AU") k.AU = v;
+        else if (K == "EMRAT") k.EMRAT = v;
+        else if (K == "J2E") k.J2E = v;
+        else if (K == "J3E") k.J3E = v;
+        else if (K == "J4E") k.J4E = v;
+        else if (K == "J2SUN") k.J2SUN = v;
+        else if (K == "RE") k.RE = v;
+        else if (K == "CLIGHT") k.CLIGHT = v;
+        else if (K == "ASUN") k.ASUN = v;
+        else if (K.compare(0, 2, "GM") == 0 || K.compare(0, 2, "MA") == 0) k.masses.push_back({K, v});
+    }
+    return k;
+}
+
+/* Masses of SPK targets by name (src/spk.c:137-200): planets from GMS,
+ * GM1.., GMB (Earth and Moon split by EMRAT), asteroids from MAnnnn. */
+static void spk_join_masses(spk_s* s, const spk_constants& k) {
+    if (!s) return;
+    static const struct { const char* name; int code; } pc[] = {
+        {"GMS", 10}, {"GM1", 1}, {"GM2", 2}, {"GMB", 399}, {"GMB", 3}, {"GMB", 301}, {"GM4", 4},
+        {"GM5", 5}, {"GM6", 6}, {"GM7", 7}, {"GM8", 8}, {"GM9", 9}};
+    for (auto& t : s->targets) {
+        if (t.mass != 0) continue;
+        char label[64] = {0};
+        for (auto& q : pc) if (t.code == q.code) { std::snprintf(label, sizeof(label), "%s", q.name); break; }
+        if (!label[0]) std::snprintf(label, sizeof(label), "MA%04d", t.code - 2000000);
+        for (auto& m : k.masses) {
+            if (m.first != label) continue;
+            if (t.code == 399) t.mass = m.second * (k.EMRAT / (1. + k.EMRAT));
+            else if (t.code == 301) t.mass = m.second * (1. / (1. + k.EMRAT));
+            else t.mass = m.second;
+            break;
+        }
+    }
+}
+
 /* ---------------------------------------------------------------- device view */
+static void ag_ascii_view(const ascii_s* a, DevEphem& D);
+static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out);
+
+/* The planets part of the view for a planets SPK file. */
+static void spk_planets_view(const struct assist_ephem* e, DevEphem& D) {
+    const spk_s* p = e->spk_planets;
+    D.pl_spk = 1;
+    D.pspk = p->d_data;
+    D.psegs = p->d_segs;
+    D.pmeta = p->d_meta;
+    D.au_km = e->AU;
+    D.pl_cau = e->AU;
+    for (int k = 0; k <= ASSIST_BODY_NPLANETS; k++) {
+        const int idx = k < ASSIST_BODY_NPLANETS ? e->spk_target_index[k] : e->spk_emb_index;
+        D.ps_nseg[k] = 0;
+        if (idx < 0) continue;
+        const spk_target_h& t = p->targets[(size_t)idx];
+        D.ps_seg0[k] = p->seg0[(size_t)idx];
+        D.ps_nseg[k] = (int)t.one.size();
+        D.ps_beg[k] = t.beg; D.ps_end[k] = t.end; D.ps_res[k] = t.res;
+        if (k < ASSIST_BODY_NPLANETS) D.gm[k] = t.mass;
+    }
+}
+
 int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
-    if (!e || !e->ascii_planets) return ASSIST_ERROR_EPHEM_FILE;
-    const ascii_s* a = e->ascii_planets;
+    if (!e || (!e->ascii_planets && !e->spk_planets)) return ASSIST_ERROR_EPHEM_FILE;
     DevEphem D;
     std::memset(&D, 0, sizeof(D));
     D.jd_ref = e->jd_ref;
+    if (e->spk_planets) spk_planets_view(e, D);
+    else ag_ascii_view(e->ascii_planets, D);
+    return ag_finish_view(e, D, out);
+}
+
+/* The planets part of the view for a .440/.441 file. */
+static void ag_ascii_view(const ascii_s* a, DevEphem& D) {
     D.pl_data = a->d_data;
     D.pl_ndbl = (long long)a->data.size();
     D.pl_rec_len = (int)a->rec;
@@ -322,6 +428,10 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     const double l2 = std::log2(a->inc);
     D.pl_inc_pow2 = (a->inc > 0 && std::floor(l2) == l2) ? 1 : 0;
     D.pl_inv_inc = 1.0 / a->inc;
+}
+
+/* Asteroids and constants, then the device copy of the view. */
+static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out) {
     const spk_s* s = e->spk_asteroids;
     D.n_ast = 0;
     if (s) {
@@ -340,25 +450,35 @@ int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     }
     D.J2E = e->J2E; D.J3E = e->J3E; D.J4E = e->J4E; D.J2SUN = e->J2SUN;
     D.Re_eq = e->Re_eq; D.Rs_eq = e->Rs_eq; D.c_squared = e->c_squared; D.over_c_squared = e->over_c_squared;
-    ascii_s* am = e->ascii_planets;
-    if (!am->d_view && ag_cuda_check(cudaMalloc(&am->d_view, sizeof(DevEphem)), "cudaMalloc(ephemeris view)"))
+    /* the view is owned by the planets object (one view per ephemeris) */
+    DevEphem** d_view = e->spk_planets ? &e->spk_planets->d_view : &e->ascii_planets->d_view;
+    DevEphem* h_view = e->spk_planets ? &e->spk_planets->h_view : &e->ascii_planets->h_view;
+    if (!*d_view && ag_cuda_check(cudaMalloc(d_view, sizeof(DevEphem)), "cudaMalloc(ephemeris view)"))
         return ASSIST_ERROR_EPHEM_FILE;
-    D.self_dev = am->d_view;
-    if (std::memcmp(&am->h_view, &D, sizeof(D)) != 0) {
+    D.self_dev = *d_view;
+    if (std::memcmp(h_view, &D, sizeof(D)) != 0) {
         /* the view changed (first use, jd_ref or constants edited): refresh the device copy */
-        if (ag_cuda_check(cudaMemcpy(am->d_view, &D, sizeof(D), cudaMemcpyHostToDevice), "upload ephemeris view"))
+        if (ag_cuda_check(cudaMemcpy(*d_view, &D, sizeof(D), cudaMemcpyHostToDevice), "upload ephemeris view"))
             return ASSIST_ERROR_EPHEM_FILE;
-        am->h_view = D;
+        *h_view = D;
     }
     *out = D;
     return ASSIST_SUCCESS;
 }
 
 int ag_ephem_view_ready(const struct assist_ephem* e) {
-    return e && e->ascii_planets && e->ascii_planets->d_view ? 1 : 0;
+    if (!e) return 0;
+    if (e->spk_planets) return e->spk_planets->d_view ? 1 : 0;
+    return e->ascii_planets && e->ascii_planets->d_view ? 1 : 0;
 }
 
-double ag_sun_gm(const struct assist_ephem* e) { return e->ascii_planets->mass[ASSIST_BODY_SUN]; }
+double ag_sun_gm(const struct assist_ephem* e) {
+    if (e->spk_planets) {
+        const int i = e->spk_target_index[ASSIST_BODY_SUN];
+        return i >= 0 ? e->spk_planets->targets[(size_t)i].mass : 0.0;
+    }
+    return e->ascii_planets->mass[ASSIST_BODY_SUN];
+}
 
 int ag_ephem_n_bodies(const struct assist_ephem* e) {
     return ASSIST_BODY_NPLANETS + (e && e->spk_asteroids ? (int)e->spk_asteroids->targets.size() : 0);
@@ -449,13 +569,47 @@ extern "C" int assist_ephem_init(struct assist_ephem* ephem, char* user_planets_
                 ast_missing = true;
             }
         }
+    } else if (fmt == FILE_FORMAT_VALID_BSP) {
+        /* planets from an SPK file (src/assist.c:252-292) */
+        spk_s* p = spk_load(planets);
+        if (!p) {
+            spk_free(ephem->spk_asteroids);
+            ephem->spk_asteroids = nullptr;
+            return ASSIST_ERROR_EPHEM_FILE;
+        }
+        ephem->spk_planets = p;
+        ephem->planets_source = FILE_FORMAT_VALID_BSP;
+        static const int naif_by_assist[ASSIST_BODY_NPLANETS] = {10, 1, 2, 399, 301, 4, 5, 6, 7, 8, 9};
+        for (int k = 0; k < ASSIST_BODY_NPLANETS; k++)
+            for (size_t i = 0; i < p->targets.size(); i++)
+                if (p->targets[i].code == naif_by_assist[k]) { ephem->spk_target_index[k] = (int)i; break; }
+        for (size_t i = 0; i < p->targets.size(); i++)
+            if (p->targets[i].code == 3) { ephem->spk_emb_index = (int)i; break; }
+        const spk_constants k = spk_parse_constants(p->comments);
+        ephem->AU = k.AU; ephem->EMRAT = k.EMRAT; ephem->J2E = k.J2E; ephem->J3E = k.J3E; ephem->J4E = k.J4E;
+        ephem->J2SUN = k.J2SUN; ephem->RE = k.RE; ephem->CLIGHT = k.CLIGHT; ephem->ASUN = k.ASUN;
+        ephem->Re_eq = ephem->RE / ephem->AU;
+        ephem->Rs_eq = ephem->ASUN / ephem->AU;
+        ephem->c_AU_per_day = (ephem->CLIGHT / ephem->AU) * 86400;
+        ephem->c_squared = ephem->c_AU_per_day * ephem->c_AU_per_day;
+        ephem->over_c_squared = 1.0 / ephem->c_squared;
+        spk_join_masses(p, k);
+        spk_join_masses(ephem->spk_asteroids, k);
+        ephem->planets_calc = ag_planets_calc;
+        /* Earth and Moon are evaluated about the Earth-Moon barycentre */
+        if (ephem->spk_emb_index < 0 || ephem->spk_target_index[ASSIST_BODY_EARTH] < 0 ||
+            ephem->spk_target_index[ASSIST_BODY_MOON] < 0)
+            std::fprintf(stderr, "(ASSIST) Planets SPK file lacks the Earth (399), Moon (301) or Earth-Moon barycentre (3).\n");
+        if (ephem->spk_asteroids && (int)ephem->spk_asteroids->targets.size() > AG_MAX_AST) {
+            std::fprintf(stderr, "(ASSIST) Asteroid file has more than %d targets.\n", AG_MAX_AST);
+            spk_free(ephem->spk_asteroids);
+            ephem->spk_asteroids = nullptr;
+            ast_missing = true;
+        }
     } else {
         spk_free(ephem->spk_asteroids);
         ephem->spk_asteroids = nullptr;
-        if (fmt == FILE_FORMAT_VALID_BSP)
-            std::fprintf(stderr, "(ASSIST) Error: '%s' is an SPK planets file; this library evaluates planets from .440/.441 files.\n", planets);
-        else
-            std::fprintf(stderr, "(ASSIST) Error: Failed to initialize planets ephemeris from '%s'.\n", planets);
+        std::fprintf(stderr, "(ASSIST) Error: Failed to initialize planets ephemeris from '%s'.\n", planets);
         return ASSIST_ERROR_EPHEM_FILE;
     }
     if (ast_missing) std::fprintf(stderr, "(ASSIST) %s\n", assist_error_messages[ASSIST_ERROR_AST_FILE]);
@@ -465,6 +619,7 @@ extern "C" int assist_ephem_init(struct assist_ephem* ephem, char* user_planets_
 extern "C" void assist_ephem_free_pointers(struct assist_ephem* ephem) {
     if (!ephem) return;
     spk_free(ephem->spk_asteroids);
+    spk_free(ephem->spk_planets);
     ascii_free(ephem->ascii_planets);
     ephem->spk_asteroids = nullptr;
     ephem->ascii_planets = nullptr;
@@ -492,7 +647,12 @@ extern "C" struct assist_ephem* assist_ephem_create(char* planets, char* asteroi
 extern "C" void assist_ephem_time_bounds(const struct assist_ephem* ephem, double* t_beg, double* t_end) {
     if (!ephem) return;
     double beg = -INFINITY, end = INFINITY;
-    if (ephem->ascii_planets) {
+    if (ephem->spk_planets) {
+        for (auto& t : ephem->spk_planets->targets) {
+            if (t.beg > beg) beg = t.beg;
+            if (t.end < end) end = t.end;
+        }
+    } else if (ephem->ascii_planets) {
         if (ephem->ascii_planets->beg > beg) beg = ephem->ascii_planets->beg;
         if (ephem->ascii_planets->end < end) end = ephem->ascii_planets->end;
     }

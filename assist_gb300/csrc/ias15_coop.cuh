@@ -43,9 +43,20 @@ struct AgCoopScratch {
 /* Table pass 1: column and asteroid component sums.  Returns this thread's
  * coverage status (combined by the caller's barrier). */
 __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const ForceCfg& c, double t, AgCoopScratch& S,
-                                                   int tid) {
+                                                   AgTable& T, int tid) {
     int bad = 0;
-    if (tid < 64) {
+    if (E.pl_spk) {
+        /* planets from an SPK file: one thread of warp 1 per body, full state
+         * straight into the table (src/spk.c:550-608) */
+        if (tid >= 32 && tid < 32 + AG_NPL) {
+            const int b = tid - 32;
+            double o[10];
+            if (ag_spk_planet(E, b, t, o) != AG_OK) bad = 1;
+            T.P.x[b] = o[1]; T.P.y[b] = o[2]; T.P.z[b] = o[3];
+            T.P.vx[b] = o[4]; T.P.vy[b] = o[5]; T.P.vz[b] = o[6];
+            if (b == AG_EAR && c.geocentric == 1) { T.P.ex_a[0] = o[7]; T.P.ex_a[1] = o[8]; T.P.ex_a[2] = o[9]; }
+        }
+    } else if (tid < 64) {
         const int lane = tid & 31;
         const bool w0 = tid < 32;
         if ((w0 && lane < 30) || (!w0 && lane < 3)) {
@@ -62,7 +73,9 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
                 S.sun_v[lane] = vs;
             }
         }
-    } else {
+    }
+    if (tid >= 64) {
+        /* asteroid components (both planets formats) */
         const bool need = (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) != 0;
         for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
             double h = 0.0;
@@ -78,6 +91,16 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
  * geocentric Earth acceleration. */
 __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const ForceCfg& c, double t, AgTable& T,
                                                     const AgCoopScratch& S, int tid) {
+    if (E.pl_spk) {
+        /* planets are in place: only the barycentric asteroids */
+        if (tid >= 64)
+            for (int q = tid - 64; q < 3 * E.n_ast; q += 64) {
+                const int comp = q % 3;
+                const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
+                T.ast[q / 3][comp] = __dadd_rn(S.ast_h[q / 3][comp], sun);
+            }
+        return;
+    }
     if (tid < 33) {
         const int b = tid / 3, comp = tid % 3;
         double u;
@@ -462,7 +485,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             const bool last = live && last_group && rem == rem_min;
 
             /* ---- node 0: accelerations at the step start, g from the predicted b */
-            int bad = ag_coop_table_pass1(E, cf, t, S.scr, tid);
+            int bad = ag_coop_table_pass1(E, cf, t, S.scr, Tab, tid);
             if (live)
                 for (int comp = 0; comp < C; comp++)
                     if (ag_coop_owner(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
@@ -540,7 +563,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 for (int n = 1; n < 8; n++) {
                     const double hn = ag_ias.h[n];
                     const double tn = t + (tc + hstep * hn);
-                    bad = ag_coop_table_pass1(E, cf, tn, S.scr, tid);
+                    bad = ag_coop_table_pass1(E, cf, tn, S.scr, Tab, tid);
                     if (!conv) {
                         double sx[9], sv[8];
                         sx[0] = hstep * hn;

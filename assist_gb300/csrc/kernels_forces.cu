@@ -31,14 +31,25 @@ __device__ void ag_block_table(const DevEphem& E, const ForceCfg& c, double t, A
     if (tid == 0) {
         const double* rec = nullptr;
         double tf = 0.0;
-        s_st = ag_planet_record(E, t, &rec, &tf);
+        s_st = E.pl_spk ? AG_OK : ag_planet_record(E, t, &rec, &tf);
         s_rec = rec;
         s_tf = tf;
     }
     __syncthreads();
     int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
     if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
-    if (s_st == AG_OK && tid < AG_NPL) {
+    if (E.pl_spk) {
+        /* planets from an SPK file: one thread per body, full state */
+        if (tid < AG_NPL) {
+            double o[10];
+            const int st = ag_spk_planet(E, tid, t, o);
+            if (st != AG_OK) atomicMax(&s_st, st);
+            T.P.x[tid] = o[1]; T.P.y[tid] = o[2]; T.P.z[tid] = o[3];
+            T.P.vx[tid] = o[4]; T.P.vy[tid] = o[5]; T.P.vz[tid] = o[6];
+            if (tid == AG_EAR && c.geocentric == 1) { T.P.ex_a[0] = o[7]; T.P.ex_a[1] = o[8]; T.P.ex_a[2] = o[9]; }
+        }
+        __syncthreads();
+    } else if (s_st == AG_OK && tid < AG_NPL) {
         const int b = tid;
         double u[3], v[3] = {0.0, 0.0, 0.0};
         if ((b == AG_SUN) || (b < nv)) ag_planet_exact<true>(E, s_rec, s_tf, b, u, v);

@@ -509,49 +509,6 @@ __device__ __forceinline__ double warp_min(double v) {
     return v;
 }
 
-/* The body table for time t, built by the whole warp (uniform result). */
-__device__ int ag_warp_table(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
-    const double* rec = nullptr;
-    double tf = 0.0;
-    int st = ag_planet_record(E, t, &rec, &tf);
-    if (st != AG_OK) return st;
-    int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
-    if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
-    if (lane < AG_NPL) {
-        double u[3], v[3] = {0.0, 0.0, 0.0};
-        if (lane == AG_SUN || lane < nv) ag_planet_exact<true>(E, rec, tf, lane, u, v);
-        else ag_planet_exact<false>(E, rec, tf, lane, u, v);
-        T.P.x[lane] = u[0]; T.P.y[lane] = u[1]; T.P.z[lane] = u[2];
-        T.P.vx[lane] = v[0]; T.P.vy[lane] = v[1]; T.P.vz[lane] = v[2];
-        if (lane == AG_EAR && c.geocentric == 1) {
-            double e_[10];
-            ag_planet_full(E, AG_EAR, t, e_);
-            T.P.ex_a[0] = e_[7]; T.P.ex_a[1] = e_[8]; T.P.ex_a[2] = e_[9];
-        }
-    }
-    __syncwarp();
-    int ast_st = AG_OK;
-    if (lane >= AG_NPL)
-        for (int m = lane - AG_NPL; m < E.n_ast; m += 32 - AG_NPL) {
-            double h[3];
-            const int s2 = ag_asteroid_exact(E, m, t, h);
-            if (s2 != AG_OK) ast_st = s2;
-            T.ast[m][0] = __dadd_rn(h[0], T.P.x[AG_SUN]);
-            T.ast[m][1] = __dadd_rn(h[1], T.P.y[AG_SUN]);
-            T.ast[m][2] = __dadd_rn(h[2], T.P.z[AG_SUN]);
-        }
-    if ((c.forces & AG_F_EIH) && lane < c.gr_eih_sources && lane < AG_NPL) {
-        double aj[3], t1;
-        ag_eih_source(E, T.P, lane, aj, &t1);
-        T.eih_a[lane][0] = aj[0]; T.eih_a[lane][1] = aj[1]; T.eih_a[lane][2] = aj[2]; T.eih_t1[lane] = t1;
-    }
-    if (!(c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST))) ast_st = AG_OK;
-    __syncwarp();
-    const unsigned bad = __ballot_sync(AG_FULL, ast_st != AG_OK);
-    T.status = AG_OK;
-    return bad ? AG_ERR_COVERAGE : AG_OK;
-}
-
 template <int NV>
 __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);

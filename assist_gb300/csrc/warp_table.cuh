@@ -100,11 +100,75 @@ __device__ __noinline__ void ag_table_earth_acc(const DevEphem& E, double t, AgT
     T.P.ex_a[0] = e_[7]; T.P.ex_a[1] = e_[8]; T.P.ex_a[2] = e_[9];
 }
 
+/* Asteroids (barycentric, from the table's Sun) and the EIH per-source sums
+ * of a table whose planets are in place; warp-uniform status. */
+__device__ __forceinline__ int ag_warp_table_rest(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
+    /* ---- phase C: asteroid components (3 lanes per asteroid) */
+    int ast_st = AG_OK;
+    for (int task = lane; task < 3 * E.n_ast; task += 32) {
+        const int m = task / 3, comp = task % 3;
+        double h;
+        const int s2 = ag_astcomp_exact(E, m, comp, t, &h);
+        if (s2 != AG_OK) ast_st = s2;
+        const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
+        T.ast[m][comp] = __dadd_rn(h, sun);
+    }
+    __syncwarp();
+    /* ---- phase D: per-source EIH sums, one lane per other planet */
+    if (c.forces & AG_F_EIH) {
+        for (int j = 0; j < c.gr_eih_sources && j < AG_NPL; j++) {
+            double ax = 0.0, ay = 0.0, az = 0.0, s1 = 0.0;
+            if (lane < AG_NPL && lane != j) {
+                const int k = lane;
+                const double dx = T.P.x[j] - T.P.x[k], dy = T.P.y[j] - T.P.y[k], dz = T.P.z[j] - T.P.z[k];
+                const double ri = rsqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+                const double gri = E.gm[k] * ri;
+                s1 = gri;
+                const double f = gri * ri * ri;
+                ax = -f * dx; ay = -f * dy; az = -f * dz;
+            }
+            for (int o = 8; o > 0; o >>= 1) {
+                ax += __shfl_down_sync(0xffffffffu, ax, o, 16);
+                ay += __shfl_down_sync(0xffffffffu, ay, o, 16);
+                az += __shfl_down_sync(0xffffffffu, az, o, 16);
+                s1 += __shfl_down_sync(0xffffffffu, s1, o, 16);
+            }
+            if (lane == 0) { T.eih_a[j][0] = ax; T.eih_a[j][1] = ay; T.eih_a[j][2] = az; T.eih_t1[j] = s1; }
+        }
+    }
+    if (!(c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST))) ast_st = AG_OK;
+    __syncwarp();
+    const unsigned bad = __ballot_sync(0xffffffffu, ast_st != AG_OK);
+    if (lane == 0) T.status = AG_OK;
+    __syncwarp();
+    return bad ? AG_ERR_COVERAGE : AG_OK;
+}
+
+/* The planets of the table from a planets SPK file: one lane per body, full
+ * state (src/spk.c:550-608).  Returns a warp-uniform status. */
+__device__ __noinline__ int ag_warp_planets_spk(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
+    int st = AG_OK;
+    if (lane < AG_NPL) {
+        double o[10];
+        st = ag_spk_planet(E, lane, t, o);
+        T.P.x[lane] = o[1]; T.P.y[lane] = o[2]; T.P.z[lane] = o[3];
+        T.P.vx[lane] = o[4]; T.P.vy[lane] = o[5]; T.P.vz[lane] = o[6];
+        if (lane == AG_EAR && c.geocentric == 1) { T.P.ex_a[0] = o[7]; T.P.ex_a[1] = o[8]; T.P.ex_a[2] = o[9]; }
+    }
+    __syncwarp();
+    return __any_sync(0xffffffffu, st != AG_OK) ? AG_ERR_COVERAGE : AG_OK;
+}
+
 /* Build the table of time t with the whole warp.  Returns a warp-uniform
  * status.  Falls back to body-per-lane velocities when more EIH sources than
  * the Sun need velocities (rare configuration). */
 __device__ __noinline__ int ag_warp_table_fast(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, AgWarpScratch& S,
                                   int lane) {
+    if (E.pl_spk) {
+        const int sp = ag_warp_planets_spk(E, c, t, T, lane);
+        if (sp != AG_OK) return sp;
+        return ag_warp_table_rest(E, c, t, T, lane);
+    }
     const double* rec = nullptr;
     double tf = 0.0;
     int st = ag_planet_record(E, t, &rec, &tf);
@@ -150,45 +214,7 @@ __device__ __noinline__ int ag_warp_table_fast(const DevEphem& E, const ForceCfg
     __syncwarp();
     if (nv > 1 && lane > 0 && lane < nv && lane < AG_NPL) ag_table_velocity(E, rec, tf, lane, T);
     if (c.geocentric == 1 && lane == AG_EAR) ag_table_earth_acc(E, t, T);
-    /* ---- phase C: asteroid components (3 lanes per asteroid) */
-    int ast_st = AG_OK;
-    for (int task = lane; task < 3 * E.n_ast; task += 32) {
-        const int m = task / 3, comp = task % 3;
-        double h;
-        const int s2 = ag_astcomp_exact(E, m, comp, t, &h);
-        if (s2 != AG_OK) ast_st = s2;
-        const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
-        T.ast[m][comp] = __dadd_rn(h, sun);
-    }
-    __syncwarp();
-    /* ---- phase D: per-source EIH sums, one lane per other planet */
-    if (c.forces & AG_F_EIH) {
-        for (int j = 0; j < c.gr_eih_sources && j < AG_NPL; j++) {
-            double ax = 0.0, ay = 0.0, az = 0.0, s1 = 0.0;
-            if (lane < AG_NPL && lane != j) {
-                const int k = lane;
-                const double dx = T.P.x[j] - T.P.x[k], dy = T.P.y[j] - T.P.y[k], dz = T.P.z[j] - T.P.z[k];
-                const double ri = rsqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
-                const double gri = E.gm[k] * ri;
-                s1 = gri;
-                const double f = gri * ri * ri;
-                ax = -f * dx; ay = -f * dy; az = -f * dz;
-            }
-            for (int o = 8; o > 0; o >>= 1) {
-                ax += __shfl_down_sync(0xffffffffu, ax, o, 16);
-                ay += __shfl_down_sync(0xffffffffu, ay, o, 16);
-                az += __shfl_down_sync(0xffffffffu, az, o, 16);
-                s1 += __shfl_down_sync(0xffffffffu, s1, o, 16);
-            }
-            if (lane == 0) { T.eih_a[j][0] = ax; T.eih_a[j][1] = ay; T.eih_a[j][2] = az; T.eih_t1[j] = s1; }
-        }
-    }
-    if (!(c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST))) ast_st = AG_OK;
-    __syncwarp();
-    const unsigned bad = __ballot_sync(0xffffffffu, ast_st != AG_OK);
-    if (lane == 0) T.status = AG_OK;
-    __syncwarp();
-    return bad ? AG_ERR_COVERAGE : AG_OK;
+    return ag_warp_table_rest(E, c, t, T, lane);
 }
 
 #endif

@@ -60,6 +60,15 @@ def synth_files(tmp_path_factory):
     return pl, ast, system
 
 
+@pytest.fixture(scope="session")
+def synth_files_spk(synth_files, tmp_path_factory):
+    """The same synthetic planets as an SPK file (with the same asteroids)."""
+    from assist_gb300 import synth
+    pl, ast, system = synth_files
+    d = str(tmp_path_factory.mktemp("synth_spk"))
+    return synth.write_planets_spk(d, system, 7, 7800.0, 9000.0), ast, system
+
+
 def rel_err(a, b):
     """Per-row ||a - b|| / ||b|| (the 1e-14 acceleration criterion)."""
     a = np.asarray(a).reshape(-1, 3)

@@ -195,3 +195,24 @@ def test_batch_geocentric_vs_oracle(synth_files, group_steps):
     assert np.array_equal(status, rstat)
     ok = rstat == 0
     assert np.abs(out[ok, :3] - ref[ok, :3]).max() < 1e-9
+
+
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
+def test_batch_spk_planets_vs_oracle(synth_files_spk, group_steps):
+    """Planets from an SPK file (ASSIST's default de440.bsp layout: Earth and
+    Moon about the Earth-Moon barycentre, constants from the comment area):
+    every batched kernel against the oracle."""
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files_spk
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "mix", 256, seed=17, t0=8000.0, log_len=(30.0, 600.0), nongrav_frac=0.1)
+    o = batch.options(group_steps=group_steps)
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params, opts=o)
+    ref, _, rstat, _ = O.integrate_batch(pop.t0, pop.t_end, pop.state, params=pop.params, return_all=True)
+    assert np.array_equal(status, rstat)
+    ok = rstat == 0
+    dx = np.abs(out[ok, :3] - ref[ok, :3]).max(axis=1)
+    assert dx.max() < 1e-9, dx.max()
+    if group_steps == 0:
+        assert np.median(dx) < 1e-12

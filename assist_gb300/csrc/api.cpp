@@ -435,8 +435,6 @@ extern "C" int reb_simulation_integrate(struct reb_simulation* r, double tmax) {
 /* One step of size r->dt (possibly retried with a smaller one after a
  * rejection): integrate to t + dt without forcing the end time. */
 extern "C" void reb_simulation_step(struct reb_simulation* r) {
-    struct assist_extras* ax = (struct assist_extras*)r->extras;
-    (void)ax;
     integrate_device(r, r->t + r->dt, 1, false);
 }
 

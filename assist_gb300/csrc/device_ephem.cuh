@@ -40,6 +40,12 @@ struct AgSpkSeg {
     int meta_off;                /* index of the first record in rec_meta */
 };
 
+/* Per SPK record: x = MID as a Julian date, y = RADIUS/86400 (days),
+ * z = 86400/RADIUS, w unused (32-byte aligned for one vector load). */
+struct __align__(32) AgRecMeta {
+    double x, y, z, w;
+};
+
 /* Everything a kernel needs to evaluate bodies; passed by value. */
 struct DevEphem {
     double jd_ref;
@@ -64,7 +70,7 @@ struct DevEphem {
     double ast_beg[AG_MAX_AST], ast_end[AG_MAX_AST], ast_res[AG_MAX_AST], ast_gm[AG_MAX_AST];
     int ast_nseg[AG_MAX_AST], ast_seg0[AG_MAX_AST];
     const struct AgSpkSeg* segs; /* per segment, see AgSpkSeg */
-    const double4* rec_meta;     /* per SPK record: (MID as JD, RADIUS/86400, 86400/RADIUS, 0) */
+    const AgRecMeta* rec_meta;     /* per SPK record: (MID as JD, RADIUS/86400, 86400/RADIUS, 0) */
     /* planets from an SPK file (pl_spk = 1) instead of the .440 record:
      * segments of the eleven bodies' targets (Sun 10, Mercury 1, Venus 2,
      * Earth 399, Moon 301, Mars 4 .. Pluto 9) and, in slot 11, the Earth-Moon
@@ -72,7 +78,7 @@ struct DevEphem {
     int pl_spk;
     const double* pspk;          /* the whole planets SPK file as doubles */
     const struct AgSpkSeg* psegs;
-    const double4* pmeta;
+    const AgRecMeta* pmeta;
     int ps_seg0[AG_NPL + 1], ps_nseg[AG_NPL + 1];
     double ps_beg[AG_NPL + 1], ps_end[AG_NPL + 1], ps_res[AG_NPL + 1];
     double au_km;                /* the file's AU (km) */
@@ -181,7 +187,7 @@ __device__ __forceinline__ int ag_asteroid_pos(const DevEphem& E, int m, double 
     int b = (int)(((E.jd_ref - sg.init_jd) + t) * sg.inv_intlen_days);
     if (b >= sg.nrec) b = sg.nrec - 1;
     if (b < 0) b = 0;
-    const double4 meta = E.rec_meta[sg.meta_off + b];
+    const AgRecMeta meta = E.rec_meta[sg.meta_off + b];
     const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2;
     const int P = sg.P;
     const double z = ((E.jd_ref - meta.x) + t) * meta.z;
@@ -306,7 +312,7 @@ __device__ __forceinline__ void ag_column_pva_exact(const DevEphem& E, const dou
     }
 }
 
-__device__ inline int ag_spk_planet(const DevEphem& E, int body, double t, double* out);
+static __device__ __noinline__ int ag_spk_planet(const DevEphem& E, int body, double t, double* out);
 
 __device__ inline int ag_planet_full(const DevEphem& E, int body, double t, double* out) {
     if (E.pl_spk) return ag_spk_planet(E, body, t, out);
@@ -343,7 +349,7 @@ __device__ inline int ag_planet_full(const DevEphem& E, int body, double t, doub
  * assist_spk_target_pos (src/spk.c:492-548): segment n from the target's
  * begin epoch and step, record b from the segment directory, z from the
  * record's MID and RADIUS, T/S/U recurrences, c = 1/RADIUS[s]. */
-__device__ inline void ag_spk_target_pva(const DevEphem& E, int slot, double t, double* u, double* v, double* w) {
+static __device__ __noinline__ void ag_spk_target_pva(const DevEphem& E, int slot, double t, double* u, double* v, double* w) {
     int n = (int)__ddiv_rn(__dsub_rn(__dadd_rn(E.jd_ref, t), E.ps_beg[slot]), E.ps_res[slot]);
     if (n >= E.ps_nseg[slot]) n = E.ps_nseg[slot] - 1;
     if (n < 0) n = 0;
@@ -351,7 +357,7 @@ __device__ inline void ag_spk_target_pva(const DevEphem& E, int slot, double t, 
     int b = (int)(__ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, sg.init_jd), t), sg.intlen_days));
     if (b >= sg.nrec) b = sg.nrec - 1;
     if (b < 0) b = 0;
-    const double4 meta = E.pmeta[sg.meta_off + b];
+    const AgRecMeta meta = E.pmeta[sg.meta_off + b];
     const double* val = E.pspk + sg.data_off + (size_t)b * sg.R;
     const int P = sg.P;
     const double z = __ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, meta.x), t), meta.y);
@@ -381,7 +387,7 @@ __device__ inline void ag_spk_target_pva(const DevEphem& E, int slot, double t, 
  * assist_spk_calc_planets_from_target forms it (src/spk.c:550-608): Earth
  * and Moon plus the Earth-Moon barycentre, then km -> AU, AU/day, AU/day^2.
  * out: GM, x,y,z, vx,vy,vz, ax,ay,az. */
-__device__ inline int ag_spk_planet(const DevEphem& E, int body, double t, double* out) {
+static __device__ __noinline__ int ag_spk_planet(const DevEphem& E, int body, double t, double* out) {
     const double jd = E.jd_ref + t;
     out[0] = E.gm[body];
     if (E.ps_nseg[body] <= 0) return AG_ERR_NEPHEM;
@@ -417,7 +423,7 @@ __device__ __forceinline__ int ag_asteroid_exact(const DevEphem& E, int m, doubl
     int b = (int)(__ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, sg.init_jd), t), sg.intlen_days));
     if (b >= sg.nrec) b = sg.nrec - 1;
     if (b < 0) b = 0;
-    const double4 meta = E.rec_meta[sg.meta_off + b];
+    const AgRecMeta meta = E.rec_meta[sg.meta_off + b];
     const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2;
     const int P = sg.P;
     const double z = __ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, meta.x), t), meta.y);

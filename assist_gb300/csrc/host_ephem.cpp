@@ -65,12 +65,12 @@ struct spk_s {
     std::vector<spk_target_h> targets;
     std::vector<double> data;
     std::vector<AgSpkSeg> segs;
-    std::vector<double4> meta;
+    std::vector<AgRecMeta> meta;
     std::vector<int> seg0;
     std::string comments;            /* comment area, NUL -> newline */
     double* d_data = nullptr;
     AgSpkSeg* d_segs = nullptr;
-    double4* d_meta = nullptr;
+    AgRecMeta* d_meta = nullptr;
     DevEphem* d_view = nullptr;      /* planets files: device copy of the last view */
     DevEphem h_view;
 };
@@ -279,7 +279,7 @@ static spk_s* spk_load(const char* path) {
             g.meta_off = (int)s->meta.size();
             for (int r = 0; r < g.nrec; r++) {
                 const double* val = s->data.data() + (one - 1) + (size_t)r * g.R;
-                double4 m;
+                AgRecMeta m;
                 m.x = 2451545.0 + val[0] / 86400.0;
                 m.y = val[1] / 86400.0;
                 m.z = 1.0 / m.y;
@@ -293,8 +293,8 @@ static spk_s* spk_load(const char* path) {
               !ag_cuda_check(cudaMemcpy(s->d_data, s->data.data(), s->data.size() * 8, cudaMemcpyHostToDevice), "upload SPK") &&
               !ag_cuda_check(cudaMalloc(&s->d_segs, sizeof(AgSpkSeg) * (s->segs.size() + 1)), "cudaMalloc(SPK segments)") &&
               !ag_cuda_check(cudaMemcpy(s->d_segs, s->segs.data(), sizeof(AgSpkSeg) * s->segs.size(), cudaMemcpyHostToDevice), "upload segments") &&
-              !ag_cuda_check(cudaMalloc(&s->d_meta, sizeof(double4) * (s->meta.size() + 1)), "cudaMalloc(SPK records)") &&
-              !ag_cuda_check(cudaMemcpy(s->d_meta, s->meta.data(), sizeof(double4) * s->meta.size(), cudaMemcpyHostToDevice), "upload records");
+              !ag_cuda_check(cudaMalloc(&s->d_meta, sizeof(AgRecMeta) * (s->meta.size() + 1)), "cudaMalloc(SPK records)") &&
+              !ag_cuda_check(cudaMemcpy(s->d_meta, s->meta.data(), sizeof(AgRecMeta) * s->meta.size(), cudaMemcpyHostToDevice), "upload records");
     if (!ok) {
         if (s->d_data) cudaFree(s->d_data);
         if (s->d_segs) cudaFree(s->d_segs);

@@ -68,7 +68,7 @@ __device__ __forceinline__ int ag_astcomp_exact(const DevEphem& E, int m, int co
     int b = (int)(__ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, sg.init_jd), t), sg.intlen_days));
     if (b >= sg.nrec) b = sg.nrec - 1;
     if (b < 0) b = 0;
-    const double4 meta = E.rec_meta[sg.meta_off + b];
+    const AgRecMeta meta = E.rec_meta[sg.meta_off + b];
     const int P = sg.P;
     const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2 + comp * P;
     const double z = __ddiv_rn(__dadd_rn(__dsub_rn(E.jd_ref, meta.x), t), meta.y);

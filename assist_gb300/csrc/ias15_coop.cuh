@@ -13,6 +13,9 @@
  *   warp 1  EIH/PPN relativity (its per-source sums too), GR potential/simple
  *   warp 2  first half of the asteroids, Earth J2-J4
  *   warp 3  second half of the asteroids, Sun J2
+ * Warps 0 and 1 both need the eleven particle-planet separations: each forms
+ * half and they exchange them through shared memory at a named barrier
+ * (without Jacobians; with them each warp forms all eleven).
  *
  * The partial accelerations (and partial Jacobians) meet in shared memory and
  * are summed in a fixed order ((w3 + w2) + w1) + w0, so the planets' terms,
@@ -39,6 +42,34 @@ struct AgCoopScratch {
     double sun_v[3];                /* Sun velocity sums (km/s) */
     double ast_h[AG_MAX_AST][3];    /* heliocentric asteroid positions (AU) */
 };
+
+/* One component of a .440 column: the position sum in the reference's exact
+ * arithmetic, the velocity sum with fused multiply-adds (the table's Sun
+ * velocity enters only the relativistic and non-gravitational terms, where
+ * its last-bit rounding is below 1e-24 of the acceleration). */
+__device__ __forceinline__ double ag_colcomp_pos_vfma(const DevEphem& E, const double* rec, int col, int comp, double tf,
+                                                      double* vsum) {
+    const int ncf = E.col_ncf[col], niv = E.col_niv[col];
+    const double tt = __dmul_rn(tf, (double)niv);
+    const double fl = floor(tt);
+    int b = (int)tt;
+    if (b >= niv) b = niv - 1;
+    const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
+    const double two_t0 = __dmul_rn(2.0, t0);
+    const double* P = rec + E.col_off[col] + ncf * (3 * b + comp);
+    double u = __dadd_rn(__dmul_rn(1.0, P[0]), 0.0), v = P[1];
+    u = __dadd_rn(u, __dmul_rn(t0, P[1]));
+    double T0 = 1.0, T1 = t0, S0 = 0.0, S1 = 1.0;
+    for (int p = 2; p < ncf; p++) {
+        const double Tp = __dsub_rn(__dmul_rn(two_t0, T1), T0);
+        const double Sp = fma(two_t0, S1, fma(2.0, T1, -S0));
+        u = __dadd_rn(u, __dmul_rn(Tp, P[p]));
+        v = fma(Sp, P[p], v);
+        T0 = T1; T1 = Tp; S0 = S1; S1 = Sp;
+    }
+    *vsum = v * __ddiv_rn(__ddiv_rn((double)(niv * 2), E.pl_inc), 86400.0);
+    return u;
+}
 
 /* Table pass 1: column and asteroid component sums.  Returns this thread's
  * coverage status (combined by the caller's barrier). */
@@ -69,7 +100,7 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
                 S.col[lane / 3][lane % 3] = ag_colcomp_exact<false>(E, rec, lane / 3, lane % 3, tf, nullptr);
             } else {
                 double vs;
-                S.col[AG_C_SUN][lane] = ag_colcomp_exact<true>(E, rec, AG_C_SUN, lane, tf, &vs);
+                S.col[AG_C_SUN][lane] = ag_colcomp_pos_vfma(E, rec, AG_C_SUN, lane, tf, &vs);
                 S.sun_v[lane] = vs;
             }
         }
@@ -229,6 +260,69 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const
     return st;
 }
 
+/* Particle-planet separations split between warps 0 and 1 (bodies 0..5 and
+ * 6..10), exchanged through shared memory at named barrier 1 (64 threads:
+ * both warps wait there once per evaluation). */
+struct AgCoopSeps {
+    double d[AG_NPL][3][32];
+    double ri[AG_NPL][32];
+};
+
+/* The no-Jacobian force share of warps 0 and 1 with the separations split
+ * (every lane of both warps calls it; `active` lanes compute). */
+__device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoopSeps& SH, int lane, const AgTable& T,
+                                                      const DevEphem& E, const ForceCfg& c, const double* x,
+                                                      const double* v, const double* A, double* acc) {
+    const TableBodies B(T);
+    const PlanetState& P = T.P;
+    double xo[3], vo[3], ao[3];
+    ag_origin(c, P, xo, vo, ao);
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    const int k0 = w == 0 ? 0 : 6, k1 = w == 0 ? 6 : AG_NPL;
+    if (active)
+        for (int k = k0; k < k1; k++) {
+            double dx, dy, dz, ri;
+            ag_sep(P, x, xo, k, dx, dy, dz, ri);
+            SH.d[k][0][lane] = dx; SH.d[k][1][lane] = dy; SH.d[k][2][lane] = dz; SH.ri[k][lane] = ri;
+        }
+    __syncwarp();
+    asm volatile("bar.sync 1, 64;" ::: "memory");
+    if (active) {
+        double dx[AG_NPL], dy[AG_NPL], dz[AG_NPL], ri[AG_NPL];
+#pragma unroll
+        for (int k = 0; k < AG_NPL; k++) { dx[k] = SH.d[k][0][lane]; dy[k] = SH.d[k][1][lane]; dz[k] = SH.d[k][2][lane]; ri[k] = SH.ri[k][lane]; }
+        if (w == 0) {
+            if ((c.forces & AG_F_NONGRAV) && A != nullptr && (A[0] != 0.0 || A[1] != 0.0 || A[2] != 0.0)) {
+                const double d[3] = {dx[AG_SUN], dy[AG_SUN], dz[AG_SUN]};
+                const double dv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
+                double JA[3][3];
+                bool has_ng;
+                ag_term_nongrav<false>(c, d, ri[AG_SUN], dv, A, ax, ay, az, nullptr, JA, &has_ng);
+            }
+            if (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) {
+#pragma unroll
+                for (int q = 0; q < AG_NPL; q++) {
+                    const int k = ag_planet_order(q);
+                    const bool on = (k == AG_SUN) ? (c.forces & AG_F_SUN) : (c.forces & AG_F_PLANETS);
+                    ag_term_planet<false>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, nullptr);
+                }
+            }
+            if (c.geocentric == 1) { ax -= ao[0]; ay -= ao[1]; az -= ao[2]; }
+        } else {
+            if (c.forces & AG_F_EIH) ag_term_eih<TableBodies, false>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, nullptr);
+            if (c.forces & (AG_F_GR_POT | AG_F_GR_SIMPLE)) {
+                const double p[3] = {dx[AG_SUN], dy[AG_SUN], dz[AG_SUN]};
+                if (c.forces & AG_F_GR_POT) ag_term_gr_pot<false>(E, p, ri[AG_SUN], ax, ay, az, nullptr);
+                if (c.forces & AG_F_GR_SIMPLE) {
+                    const double pv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
+                    ag_term_gr_simple<false>(E, p, ri[AG_SUN], pv, ax, ay, az, nullptr);
+                }
+            }
+        }
+    }
+    acc[0] = ax; acc[1] = ay; acc[2] = az;
+}
+
 /* b, e of one component from the last accepted step's br, er (the shift of
  * the acceleration polynomial to the new step). */
 template <int C>
@@ -272,6 +366,7 @@ struct AgCoopShared {
     AgCoopScratch scr;
     double xs[C][32], vs[C][32];                    /* state at the current node */
     double pa[4][3][32];                            /* partial accelerations */
+    typename std::conditional<NV == 0, AgCoopSeps, char>::type seps;   /* warp 0 <-> warp 1 separations */
     double pj[NV > 0 ? 4 : 1][NV > 0 ? 18 : 1][32]; /* partial Jacobians */
     double ra[3][32], rdb[3][32];                   /* |a|, |delta b6| of x, y, z at node 7 */
     double rb6[3][32];                              /* |b6| of x, y, z after convergence */
@@ -495,20 +590,27 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             __syncthreads();
             if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
             int fst = AG_OK;
-            if (live) {
+            {
                 const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
                 const double vp[3] = {S.vs[0][lane], S.vs[1][lane], S.vs[2][lane]};
-                double acc[3];
+                double acc[3] = {0.0, 0.0, 0.0};
                 if (NV > 0) {
-                    double J[3][6];
-                    fst = ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
-                    for (int a = 0; a < 3; a++)
-                        for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
-                } else {
+                    if (live) {
+                        double J[3][6];
+                        fst = ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
+                        for (int a = 0; a < 3; a++)
+                            for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
+                    }
+                } else if (wid < 2) {
+                    if constexpr (NV == 0)
+                        ag_coop_force_split01(wid, live, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
+                } else if (live) {
                     fst = ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
                 }
-                S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
-                if (wid == 0) n_ev++;
+                if (live) {
+                    S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
+                    if (wid == 0) n_ev++;
+                }
             }
             bad = __syncthreads_or(fst != AG_OK);
             if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
@@ -593,20 +695,27 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     ag_coop_table_pass2(E, cf, tn, Tab, S.scr, tid);
                     __syncthreads();
                     if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
-                    if (!conv) {
+                    {
                         const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
                         const double vp[3] = {S.vs[0][lane], S.vs[1][lane], S.vs[2][lane]};
-                        double acc[3];
+                        double acc[3] = {0.0, 0.0, 0.0};
                         if (NV > 0) {
-                            double J[3][6];
-                            ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
-                            for (int a = 0; a < 3; a++)
-                                for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
-                        } else {
+                            if (!conv) {
+                                double J[3][6];
+                                ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
+                                for (int a = 0; a < 3; a++)
+                                    for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
+                            }
+                        } else if (wid < 2) {
+                            if constexpr (NV == 0)
+                                ag_coop_force_split01(wid, !conv, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
+                        } else if (!conv) {
                             ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
                         }
-                        S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
-                        if (wid == 0) n_ev++;
+                        if (!conv) {
+                            S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
+                            if (wid == 0) n_ev++;
+                        }
                     }
                     __syncthreads();
                     if (!conv) {

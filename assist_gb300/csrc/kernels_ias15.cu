@@ -34,6 +34,8 @@
 #include <cmath>
 #include <cstdio>
 
+#include <type_traits>
+
 #include "device_forces.cuh"
 #include "ias15_constants.h"
 #include "internal.h"

@@ -362,7 +362,9 @@ __device__ __forceinline__ int ag_coop_owner(int comp) {
 template <int NV>
 struct AgCoopShared {
     static constexpr int C = 3 * (1 + NV);
-    AgTable tab;
+    AgTable tab[NV == 0 ? 8 : 1];   /* body tables; without Jacobians one per node, kept through the
+                                       predictor-corrector iterations of a step (the node times do
+                                       not change while it iterates) */
     AgCoopScratch scr;
     double xs[C][32], vs[C][32];                    /* state at the current node */
     double pa[4][3][32];                            /* partial accelerations */
@@ -461,12 +463,15 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     const DevEphem& E = *Ep;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     __shared__ AgCoopShared<NV> S;
-    AgTable& Tab = S.tab;
+    AgTable& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
     const Ws<C> W{A.ws, A.nslots, slot};
     const long long clk0 = clock64();
     unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
-    if (tid == 0) { Tab.status = AG_OK; S.stop = 0; }
+    if (tid == 0) {
+        for (int k = 0; k < (NV == 0 ? 8 : 1); k++) S.tab[k].status = AG_OK;
+        S.stop = 0;
+    }
     /* learned warm start and step logging (no variational particles) */
     extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
     AgWarmSmem& WS = *reinterpret_cast<AgWarmSmem*>(ag_dyn_smem);
@@ -665,7 +670,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 for (int n = 1; n < 8; n++) {
                     const double hn = ag_ias.h[n];
                     const double tn = t + (tc + hstep * hn);
-                    bad = ag_coop_table_pass1(E, cf, tn, S.scr, Tab, tid);
+                    AgTable& TabN = S.tab[NV == 0 ? n : 0];
+                    const bool build = NV != 0 || iters == 1;     /* block-uniform */
+                    bad = build ? ag_coop_table_pass1(E, cf, tn, S.scr, TabN, tid) : 0;
                     if (!conv) {
                         double sx[9], sv[8];
                         sx[0] = hstep * hn;
@@ -692,9 +699,11 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     }
                     bad = __syncthreads_or(bad);
                     if (bad) { cov = true; break; }
-                    ag_coop_table_pass2(E, cf, tn, Tab, S.scr, tid);
-                    __syncthreads();
-                    if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
+                    if (build) {
+                        ag_coop_table_pass2(E, cf, tn, TabN, S.scr, tid);
+                        __syncthreads();
+                        if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, TabN, lane);
+                    }
                     {
                         const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
                         const double vp[3] = {S.vs[0][lane], S.vs[1][lane], S.vs[2][lane]};
@@ -702,15 +711,15 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                         if (NV > 0) {
                             if (!conv) {
                                 double J[3][6];
-                                ag_coop_force_part<true>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
+                                ag_coop_force_part<true>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, J);
                                 for (int a = 0; a < 3; a++)
                                     for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
                             }
                         } else if (wid < 2) {
                             if constexpr (NV == 0)
-                                ag_coop_force_split01(wid, !conv, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
+                                ag_coop_force_split01(wid, !conv, S.seps, lane, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                         } else if (!conv) {
-                            ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                            ag_coop_force_part<false>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
                         }
                         if (!conv) {
                             S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];

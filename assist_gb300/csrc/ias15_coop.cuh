@@ -457,6 +457,17 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
     }
 }
 
+/* Dynamic shared memory of a block: the warm-start buffers (when present),
+ * then, without variational particles, the group's IAS15 state (40 fields
+ * x 3 components x 32 lanes, 30 KB); with them the state stays in the
+ * global workspace, indexed by slot. */
+template <int NV, bool WARM>
+struct AgCoopDyn {
+    static constexpr size_t warm = WARM ? (sizeof(AgWarmSmem) + 15) / 16 * 16 : 0;
+    static constexpr size_t ws = NV == 0 ? sizeof(double) * W_NF * 3 * 32 : 0;
+    static constexpr size_t bytes = warm + ws;
+};
+
 template <int NV, bool WARM>
 __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
@@ -465,7 +476,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     __shared__ AgCoopShared<NV> S;
     AgTable& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
-    const Ws<C> W{A.ws, A.nslots, slot};
+    extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
+    const Ws<C> W{NV == 0 ? reinterpret_cast<double*>(ag_dyn_smem + AgCoopDyn<NV, WARM>::warm) : A.ws,
+                  NV == 0 ? 32 : A.nslots, NV == 0 ? lane : slot};
     const long long clk0 = clock64();
     unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
     if (tid == 0) {
@@ -473,7 +486,6 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
         S.stop = 0;
     }
     /* learned warm start and step logging (no variational particles) */
-    extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
     AgWarmSmem& WS = *reinterpret_cast<AgWarmSmem*>(ag_dyn_smem);
     const bool warm = WARM && NV == 0 && A.mlp != nullptr;
     const bool logp = WARM && NV == 0 && A.log_x != nullptr;
@@ -644,7 +656,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             /* ---- learned warm start: features, BF16 inference, b += kappa y */
             bool w_applied = false, w_probe = false;
             if (warm || logp)
-                ag_coop_warm_start(A, W.w, A.nslots, slot, WS, Tab, lane, wid, live, warm, wl_on, hstep, dtls, steps,
+                ag_coop_warm_start(A, W.w, W.ns, W.slot, WS, Tab, lane, wid, live, warm, wl_on, hstep, dtls, steps,
                                    w_applied, w_probe, n_wused, n_wfall);
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
@@ -966,12 +978,23 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     }
 }
 
+/* Opt the kernel in to its dynamic shared memory (above the 48 KB default). */
+template <int NV, bool WARM>
+static int ag_coop_dyn_attr() {
+    if (AgCoopDyn<NV, WARM>::bytes == 0) return 0;
+    return (int)cudaFuncSetAttribute(ag_k_coop<NV, WARM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)AgCoopDyn<NV, WARM>::bytes);
+}
+
 int ag_coop_max_slots(int nv) {
     int dev = 0, sms = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (nv == 6) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false>, 128, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false>, 128, 0);
+    if (nv == 6) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false>, 128, AgCoopDyn<6, false>::bytes);
+    } else if (ag_coop_dyn_attr<0, false>() == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false>, 128, AgCoopDyn<0, false>::bytes);
+    }
     if (bps < 1) bps = 1;
     return sms * bps * 32;
 }
@@ -981,14 +1004,13 @@ int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, i
     if (e) return e;
     const int blocks = (a.nslots + 31) / 32;
     if (nv == 6) {
-        ag_k_coop<6, false><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+        ag_k_coop<6, false><<<blocks, 128, AgCoopDyn<6, false>::bytes, s>>>(E.self_dev, c, a);
     } else if (a.mlp || a.log_x) {
-        const int dyn = (int)sizeof(AgWarmSmem);
-        cudaError_t r = cudaFuncSetAttribute(ag_k_coop<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-        if (r != cudaSuccess) return (int)r;
-        ag_k_coop<0, true><<<blocks, 128, dyn, s>>>(E.self_dev, c, a);
+        if ((e = ag_coop_dyn_attr<0, true>())) return e;
+        ag_k_coop<0, true><<<blocks, 128, AgCoopDyn<0, true>::bytes, s>>>(E.self_dev, c, a);
     } else {
-        ag_k_coop<0, false><<<blocks, 128, 0, s>>>(E.self_dev, c, a);
+        if ((e = ag_coop_dyn_attr<0, false>())) return e;
+        ag_k_coop<0, false><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
     }
     return (int)cudaGetLastError();
 }

@@ -14,6 +14,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/assist.h"
@@ -645,6 +646,63 @@ extern "C" int assist_gb300_integrate_batch_dense_device(const struct assist_eph
                               d_out_start, d_out_t, d_out_state);
 }
 
+/* Run f(i0, i1) over [0, n) on up to 16 host threads (one for small n). */
+template <class F>
+static void ag_parallel_for(int n, const F& f) {
+    int nt = (int)std::thread::hardware_concurrency();
+    nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
+    if (n < 16384) nt = 1;
+    if (nt == 1) { f(0, n); return; }
+    std::vector<std::thread> th;
+    for (int k = 0; k < nt; k++) {
+        const int a = (int)((long long)n * k / nt), b = (int)((long long)n * (k + 1) / nt);
+        th.emplace_back([a, b, &f] { f(a, b); });
+    }
+    for (auto& x : th) x.join();
+}
+
+/* Sort key of one particle for grouping: start time, then class (direction,
+ * non-gravitational parameters, timescale bucket), then length (longest
+ * first), then index, a strict total order (the result does not depend on the
+ * sort algorithm). */
+struct AgGroupKey {
+    double t0;
+    unsigned cls;
+    int idx;
+    double neg_len;
+    double cost;            /* expected evaluations, L q^-0.6 */
+    bool operator<(const AgGroupKey& b) const {
+        if (t0 != b.t0) return t0 < b.t0;
+        if (cls != b.cls) return cls < b.cls;
+        if (neg_len != b.neg_len) return neg_len < b.neg_len;
+        return idx < b.idx;
+    }
+};
+
+/* Sort in chunks on host threads, then merge the chunks pairwise. */
+static void ag_parallel_sort(std::vector<AgGroupKey>& v) {
+    const int n = (int)v.size();
+    int nt = (int)std::thread::hardware_concurrency();
+    nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
+    if (n < 16384 || nt == 1) { std::sort(v.begin(), v.end()); return; }
+    std::vector<int> cut((size_t)nt + 1);
+    for (int k = 0; k <= nt; k++) cut[(size_t)k] = (int)((long long)n * k / nt);
+    {
+        std::vector<std::thread> th;
+        for (int k = 0; k < nt; k++)
+            th.emplace_back([&v, &cut, k] { std::sort(v.begin() + cut[(size_t)k], v.begin() + cut[(size_t)k + 1]); });
+        for (auto& x : th) x.join();
+    }
+    for (int w = 1; w < nt; w *= 2) {
+        std::vector<std::thread> th;
+        for (int k = 0; k + w < nt; k += 2 * w) {
+            const int lo = cut[(size_t)k], mid = cut[(size_t)(k + w)], hi = cut[(size_t)std::min(k + 2 * w, nt)];
+            th.emplace_back([&v, lo, mid, hi] { std::inplace_merge(v.begin() + lo, v.begin() + mid, v.begin() + hi); });
+        }
+        for (auto& x : th) x.join();
+    }
+}
+
 static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
                               const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
                               int n_var, double* d_var_state, int* d_status, void* stream,
@@ -686,6 +744,17 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         if (ag_cuda_check(cudaMemcpyAsync(st0.data(), d_state, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, s), "read state"))
             return ASSIST_ERROR_EPHEM_FILE;
     }
+    /* particles with non-gravitational parameters are grouped apart: a
+     * group pays for the term when any member has it */
+    std::vector<unsigned char> has_ng((size_t)n, 0);
+    if (grouped && d_params && (c.forces & AG_F_NONGRAV)) {
+        std::vector<double> prm(3 * (size_t)n);
+        if (ag_cuda_check(cudaMemcpyAsync(prm.data(), d_params, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "read params"))
+            return ASSIST_ERROR_EPHEM_FILE;
+        if (ag_cuda_check(cudaStreamSynchronize(s), "read params")) return ASSIST_ERROR_EPHEM_FILE;
+        for (int i = 0; i < n; i++)
+            has_ng[(size_t)i] = prm[3 * (size_t)i] != 0.0 || prm[3 * (size_t)i + 1] != 0.0 || prm[3 * (size_t)i + 2] != 0.0;
+    }
     if (ag_cuda_check(cudaStreamSynchronize(s), "read inputs")) return ASSIST_ERROR_EPHEM_FILE;
     std::vector<int> order((size_t)n), gstart, gsize;
     for (int i = 0; i < n; i++) order[(size_t)i] = i;
@@ -695,13 +764,14 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
         });
     } else {
-        /* groups share t0 and direction; within them particles of similar
-         * orbital timescale (perihelion distance q^1.5, quarter-octave bins)
-         * and similar length sit together; groups are queued longest first */
+        /* groups share t0, direction and whether non-gravitational
+         * parameters are present; within them particles of similar orbital
+         * timescale (perihelion distance q^1.5, quarter-octave bins) and
+         * similar length sit together; groups are queued longest first */
         const double gm = (e->ascii_planets || e->spk_planets) ? ag_sun_gm(e) : 2.9591220828411951e-04;
-        std::vector<int> bucket((size_t)n);
-        std::vector<double> qper((size_t)n);
-        for (int i = 0; i < n; i++) {
+        std::vector<AgGroupKey> key((size_t)n);
+        ag_parallel_for(n, [&](int i0, int i1) {
+        for (int i = i0; i < i1; i++) {
             const double* p = &st0[6 * (size_t)i];
             const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
             const double v2 = p[3] * p[3] + p[4] * p[4] + p[5] * p[5];
@@ -712,8 +782,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             const double inv_a = 2.0 / r - v2 / gm;
             double q = (std::fabs(inv_a) > 1e-12) ? (1.0 - ecc) / inv_a : r;
             if (!(q > 1e-4)) q = 1e-4;
-            qper[(size_t)i] = q;
-            bucket[(size_t)i] = (int)std::floor(4.0 * std::log2(std::pow(q, 1.5)));
+            int bucket = (int)std::floor(4.0 * std::log2(std::pow(q, 1.5)));
             if (o->group_order == 1) {
                 /* orbit size (half octaves of a; unbound orbits last), length
                  * (factors of 2), then mean anomaly in 1/64 turns */
@@ -729,29 +798,39 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
                     bm = (int)std::floor(64.0 * M / (2.0 * M_PI));
                 }
                 const int bl = (int)std::floor(std::log2(std::max(L, 1e-3)));
-                bucket[(size_t)i] = ((ba + 2000) * 64 + (bl + 32)) * 64 + bm;
+                bucket = ((ba + 2000) * 64 + (bl + 32)) * 64 + bm;
             }
+            /* class bits: 31 backward, 30 non-gravitational, 0..29 bucket */
+            const double L = std::fabs(te[(size_t)i] - t0[(size_t)i]);
+            AgGroupKey& k = key[(size_t)i];
+            k.t0 = t0[(size_t)i];
+            k.cls = ((te[(size_t)i] >= t0[(size_t)i]) ? 0u : (1u << 31)) | (has_ng[(size_t)i] ? (1u << 30) : 0u) |
+                    ((unsigned)(bucket + (1 << 28)) & ((1u << 30) - 1));
+            k.idx = i;
+            k.neg_len = -L;
+            k.cost = L * std::pow(q, -0.6);
         }
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            if (t0[(size_t)a] != t0[(size_t)b]) return t0[(size_t)a] < t0[(size_t)b];
-            const bool fa = te[(size_t)a] >= t0[(size_t)a], fb = te[(size_t)b] >= t0[(size_t)b];
-            if (fa != fb) return fa;
-            if (bucket[(size_t)a] != bucket[(size_t)b]) return bucket[(size_t)a] < bucket[(size_t)b];
-            return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
         });
+        ag_parallel_sort(key);
+        for (int i = 0; i < n; i++) order[(size_t)i] = key[(size_t)i].idx;
+        /* group_order 1 orders by its bucket but breaks groups only at start
+         * time, direction and the non-gravitational flag */
+        const unsigned brk = o->group_order == 0 ? ~0u : (3u << 30);
+        std::vector<double> gl;
         int i = 0;
         while (i < n) {
-            const int a = order[(size_t)i];
+            const AgGroupKey& a = key[(size_t)i];
+            double m = a.cost;
             int j = i + 1;
             while (j < n && j - i < 32) {
-                const int b = order[(size_t)j];
-                if (t0[(size_t)b] != t0[(size_t)a] || (te[(size_t)b] >= t0[(size_t)b]) != (te[(size_t)a] >= t0[(size_t)a]) ||
-                    (o->group_order == 0 && bucket[(size_t)b] != bucket[(size_t)a]))
-                    break;
+                const AgGroupKey& b = key[(size_t)j];
+                if (b.t0 != a.t0 || ((b.cls ^ a.cls) & brk)) break;
+                m = std::max(m, b.cost);
                 j++;
             }
             gstart.push_back(i);
             gsize.push_back(j - i);
+            gl.push_back(m);
             i = j;
         }
         /* most expensive group first: a particle's evaluations grow with its
@@ -760,16 +839,6 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
          * mixture) */
         std::vector<int> gi(gstart.size());
         for (size_t k = 0; k < gi.size(); k++) gi[k] = (int)k;
-        auto glen = [&](int g) {
-            double m = 0;
-            for (int k = 0; k < gsize[(size_t)g]; k++) {
-                const int p = order[(size_t)(gstart[(size_t)g] + k)];
-                m = std::max(m, std::fabs(te[(size_t)p] - t0[(size_t)p]) * std::pow(qper[(size_t)p], -0.6));
-            }
-            return m;
-        };
-        std::vector<double> gl(gi.size());
-        for (size_t k = 0; k < gi.size(); k++) gl[k] = glen((int)k);
         std::stable_sort(gi.begin(), gi.end(), [&](int a, int b) { return gl[(size_t)a] > gl[(size_t)b]; });
         std::vector<int> s2(gi.size()), z2(gi.size());
         for (size_t k = 0; k < gi.size(); k++) { s2[k] = gstart[(size_t)gi[k]]; z2[k] = gsize[(size_t)gi[k]]; }

@@ -233,12 +233,14 @@ __device__ __forceinline__ void ag_term_nongrav(const ForceCfg& c, const double*
                                                 double (*JA)[3], bool* has_ng) {
     const double r = 1.0 / rinv;
     double g, dgdr;
-    const double rr0 = r / c.r0;
     if (c.nongrav_rm2) {
-        const double q = 1.0 / rr0;
+        /* g = alpha (r0 / r)^2: no division (the reference's pow(r/r0, -2)
+         * and this product agree to a few units in the last place) */
+        const double q = c.r0 * rinv;
         g = c.alpha * q * q;
         dgdr = -2.0 * g * rinv;
     } else {
+        const double rr0 = r / c.r0;
         const double pn = pow(rr0, c.nn);
         g = c.alpha * pow(rr0, -c.nm) * pow(1.0 + pn, -c.nk);
         dgdr = (c.alpha / c.r0) * (-c.nm * pow(rr0, -c.nm - 1) * pow(1.0 + pn, -c.nk)

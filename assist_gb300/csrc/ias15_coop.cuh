@@ -9,10 +9,14 @@
  * (each has its own FP64 pipe):
  *
  *   warp 0  planets' direct gravity (ASSIST's order, Sun last), Marsden
- *           non-gravitational term, geocentric indirect term
+ *           non-gravitational term, Earth J2-J4, geocentric indirect term
  *   warp 1  EIH/PPN relativity (its per-source sums too), GR potential/simple
- *   warp 2  first half of the asteroids, Earth J2-J4
+ *   warp 2  first half of the asteroids
  *   warp 3  second half of the asteroids, Sun J2
+ * (with variational particles, whose Jacobians fill warp 0's registers,
+ * Earth J2-J4 stays on warp 2).  Batches are grouped so that particles with
+ * non-gravitational parameters share groups: a group whose members have none
+ * skips warp 0's costliest term.
  * Warps 0 and 1 both need the eleven particle-planet separations: each forms
  * half and they exchange them through shared memory at a named barrier
  * (without Jacobians; with them each warp forms all eleven).
@@ -24,7 +28,8 @@
  * record and asteroid components of the SPK records on different threads, in
  * the reference's exact arithmetic.  Each IAS15 state component has an owner
  * warp that predicts it, forms its acceleration from the partials and
- * updates its g, b and e: x, y, z belong to warps 1, 2, 3; the three
+ * updates its g, b and e: x, y, z belong to warps 0, 2, 3 (warps 1, 2, 3
+ * with variational particles); the three
  * components of a variational particle share one warp (its J.dx product reads
  * only its own predicted values).
  * Per-particle control values (t, dt, convergence, retirement) are computed
@@ -245,7 +250,7 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const
         if (direct && (on_ast || JAC))
             st = ag_term_asteroids<TableBodies, JAC>(B, E, on_ast, x, xo, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay,
                                                      az, J);
-        if (w == 2 && (c.forces & AG_F_EARTH_H)) {
+        if (JAC && w == 2 && (c.forces & AG_F_EARTH_H)) {
             double dx, dy, dz, ri;
             ag_sep(P, x, xo, AG_EAR, dx, dy, dz, ri);
             ag_term_earth_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
@@ -307,6 +312,8 @@ __device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoop
                     ag_term_planet<false>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, nullptr);
                 }
             }
+            if (c.forces & AG_F_EARTH_H)
+                ag_term_earth_h<false>(E, c, dx[AG_EAR], dy[AG_EAR], dz[AG_EAR], ri[AG_EAR], ax, ay, az, nullptr);
             if (c.geocentric == 1) { ax -= ao[0]; ay -= ao[1]; az -= ao[2]; }
         } else {
             if (c.forces & AG_F_EIH) ag_term_eih<TableBodies, false>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, nullptr);
@@ -351,12 +358,19 @@ __device__ __forceinline__ void ag_predict_next_comp(const Ws<C>& W, int comp, d
     }
 }
 
-/* Owner warp of IAS15 component comp: x, y, z -> warps 1..3; variational
- * particles 0..5 -> warps 0, 0, 1, 2, 3, 1. */
+/* Owner warp of IAS15 component comp: x, y, z -> warps 0, 2, 3 (warps
+ * 1..3 with variational particles, which go to warps 0, 0, 1, 2, 3, 1). */
+template <int NV>
 __device__ __forceinline__ int ag_coop_owner(int comp) {
-    if (comp < 3) return comp + 1;
+    if (comp < 3) return NV == 0 ? (comp == 0 ? 0 : comp + 1) : comp + 1;
     const int q = (comp - 3) / 3;
     return q < 2 ? 0 : ((q == 2 || q == 5) ? 1 : (q == 3 ? 2 : 3));
+}
+
+/* Position component owned by warp w (-1: none). */
+template <int NV>
+__device__ __forceinline__ int ag_coop_pcomp(int w) {
+    return NV == 0 ? (w == 0 ? 0 : (w == 1 ? -1 : w - 1)) : w - 1;
 }
 
 template <int NV>
@@ -409,10 +423,11 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
                                                bool& w_probe, unsigned long long& n_wused,
                                                unsigned long long& n_wfall) {
     const Ws<3> W{ws, nslots, slot};
-    if (live && wid >= 1)
+    const int pc = ag_coop_pcomp<0>(wid);
+    if (live && pc >= 0)
         for (int k = 0; k < 7; k++) {
-            WS.corr[k][wid - 1][lane] = W(W_BR + k, wid - 1) - W(W_ER + k, wid - 1);
-            WS.bpa[k][wid - 1][lane] = (float)fabs(W(W_B + k, wid - 1));
+            WS.corr[k][pc][lane] = W(W_BR + k, pc) - W(W_ER + k, pc);
+            WS.bpa[k][pc][lane] = (float)fabs(W(W_B + k, pc));
         }
     __syncthreads();
     if (wid == 0) {
@@ -446,9 +461,9 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
             }
             if (ok_y) {
                 w_applied = true;
-                if (wid >= 1)
+                if (pc >= 0)
                     for (int k = 0; k < 7; k++)
-                        W(W_B + k, wid - 1) = fma(WS.kappa[k][lane], (double)WS.M.Y[lane][3 * k + wid - 1], W(W_B + k, wid - 1));
+                        W(W_B + k, pc) = fma(WS.kappa[k][lane], (double)WS.M.Y[lane][3 * k + pc], W(W_B + k, pc));
                 if (wid == 0) n_wused++;
             } else if (wid == 0) {
                 n_wfall++;
@@ -457,14 +472,16 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
     }
 }
 
-/* Dynamic shared memory of a block: the warm-start buffers (when present),
- * then, without variational particles, the group's IAS15 state (40 fields
- * x 3 components x 32 lanes, 30 KB); with them the state stays in the
- * global workspace, indexed by slot. */
+/* Dynamic shared memory of a block: the warm-start buffers (when present)
+ * or, in the plain kernel without variational particles, the group's IAS15
+ * state (40 fields x 3 components x 32 lanes, 30 KB).  Otherwise the state
+ * stays in the global workspace, indexed by slot (both would not leave room
+ * for two blocks per SM). */
 template <int NV, bool WARM>
 struct AgCoopDyn {
+    static constexpr bool ws_shared = NV == 0 && !WARM;
     static constexpr size_t warm = WARM ? (sizeof(AgWarmSmem) + 15) / 16 * 16 : 0;
-    static constexpr size_t ws = NV == 0 ? sizeof(double) * W_NF * 3 * 32 : 0;
+    static constexpr size_t ws = ws_shared ? sizeof(double) * W_NF * 3 * 32 : 0;
     static constexpr size_t bytes = warm + ws;
 };
 
@@ -477,8 +494,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     AgTable& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
     extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
-    const Ws<C> W{NV == 0 ? reinterpret_cast<double*>(ag_dyn_smem + AgCoopDyn<NV, WARM>::warm) : A.ws,
-                  NV == 0 ? 32 : A.nslots, NV == 0 ? lane : slot};
+    constexpr bool wss = AgCoopDyn<NV, WARM>::ws_shared;
+    const Ws<C> W{wss ? reinterpret_cast<double*>(ag_dyn_smem + AgCoopDyn<NV, WARM>::warm) : A.ws,
+                  wss ? 32 : A.nslots, wss ? lane : slot};
     const long long clk0 = clock64();
     unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
     if (tid == 0) {
@@ -514,7 +532,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
         if (live) {
             const double* s0 = A.state + 6 * (size_t)pid;
             for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                 double x0, v0;
                 if (comp < 3) { x0 = s0[comp]; v0 = s0[3 + comp]; }
                 else {
@@ -546,7 +564,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             if (__any_sync(AG_FULL, finish_now)) {
                 if (finish_now) {
                     for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                         const double x1 = W(W_X0, comp) + W(W_XC, comp), v1 = W(W_V0, comp) + W(W_VC, comp);
                         if (dense && comp < 3) {
                             /* times left at a completed particle are its t_end: the end
@@ -600,7 +618,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             int bad = ag_coop_table_pass1(E, cf, t, S.scr, Tab, tid);
             if (live)
                 for (int comp = 0; comp < C; comp++)
-                    if (ag_coop_owner(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
+                    if (ag_coop_owner<NV>(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
             bad = __syncthreads_or(bad);
             if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
             ag_coop_table_pass2(E, cf, t, Tab, S.scr, tid);
@@ -633,7 +651,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                     double at;
                     if (comp < 3) {
                         at = ((S.pa[3][comp][lane] + S.pa[2][comp][lane]) + S.pa[1][comp][lane]) + S.pa[0][comp][lane];
@@ -660,7 +678,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                                    w_applied, w_probe, n_wused, n_wfall);
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                     double b[7];
 #pragma unroll
                     for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);
@@ -695,7 +713,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
 #pragma unroll
                         for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * ag_ias.fv[n][k];
                         for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                             double px = sx[8] * W(W_B + 6, comp);
 #pragma unroll
                             for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, comp), px);
@@ -741,7 +759,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     __syncthreads();
                     if (!conv) {
                         for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                             double at;
                             if (comp < 3) {
                                 at = ((S.pa[3][comp][lane] + S.pa[2][comp][lane]) + S.pa[1][comp][lane]) + S.pa[0][comp][lane];
@@ -802,9 +820,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 }
             }
             /* ---- step-size control: each lane's choice, the group takes the smallest */
-            if (live && wid >= 1) {
-                const double bb = fabs(W(W_B + 6, wid - 1));
-                S.rb6[wid - 1][lane] = ag_isnormal_pos(bb) ? bb : 0.0;
+            if (live && ag_coop_pcomp<NV>(wid) >= 0) {
+                const double bb = fabs(W(W_B + 6, ag_coop_pcomp<NV>(wid)));
+                S.rb6[ag_coop_pcomp<NV>(wid)][lane] = ag_isnormal_pos(bb) ? bb : 0.0;
             }
             __syncthreads();
             double dt_new_l = 1e300, dt_nocap_l = 1e300;
@@ -851,7 +869,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 if (live) {
                     if (wid == 0) n_rej++;
                     for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                         if (dtls != 0.0) ag_predict_next_comp<C>(W, comp, dt_new / dtls);
                         else
                             for (int k = 0; k < 7; k++) { W(W_B + k, comp) = 0.0; W(W_E + k, comp) = 0.0; }
@@ -864,9 +882,9 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
              * (b_conv - b_pred) / kappa with b_pred = e + (br - er), the plain prediction */
             if (logp) {
                 const bool lg = live && WS.valid[lane] && (steps % A.log_every) == 0;
-                if (lg && wid >= 1)
+                if (lg && ag_coop_pcomp<NV>(wid) >= 0)
                     for (int k = 0; k < 7; k++) {
-                        const int c = wid - 1;
+                        const int c = ag_coop_pcomp<NV>(wid);
                         const double bp = W(W_E + k, c) + (W(W_BR + k, c) - W(W_ER + k, c));
                         WS.tgt[k][c][lane] = (float)((W(W_B + k, c) - bp) / WS.kappa[k][lane]);
                     }
@@ -911,8 +929,8 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     sv[5] = 5. * sv[4] * h / 6.;
                     sv[6] = 6. * sv[5] * h / 7.;
                     sv[7] = 7. * sv[6] * h / 8.;
-                    if (wid >= 1) {
-                        const int c = wid - 1;
+                    if (ag_coop_pcomp<NV>(wid) >= 0) {
+                        const int c = ag_coop_pcomp<NV>(wid);
                         const double b0 = W(W_B + 0, c), b1 = W(W_B + 1, c), b2 = W(W_B + 2, c), b3 = W(W_B + 3, c),
                                      b4 = W(W_B + 4, c), b5 = W(W_B + 5, c), b6 = W(W_B + 6, c);
                         const double a0 = W(W_A0, c), v0 = W(W_V0, c);
@@ -930,7 +948,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 if (wid == 0) n_acc++;
                 const double h2 = hstep * hstep;
                 for (int comp = 0; comp < C; comp++) {
-                    if (ag_coop_owner(comp) != wid) continue;
+                    if (ag_coop_owner<NV>(comp) != wid) continue;
                     double b[7];
 #pragma unroll
                     for (int k = 0; k < 7; k++) b[k] = W(W_B + k, comp);

@@ -334,10 +334,11 @@ def main():
     kernel_s = stats_acc["kernel_ms"] / 1e3
     peak = batch.fp64_peak_gflops() * 1e9
     achieved = flops / kernel_s
-    # DRAM bytes per launch: 0.578 B per particle-day, from one ncu capture of
-    # this kernel on the 8,192-particle case of this workload (dram__bytes_read
-    # + dram__bytes_write), scaled by the particle-days of a full launch
-    traffic = 0.578 * pdays
+    # DRAM bytes per launch: 0.318 B per particle-day, from one ncu capture of
+    # this kernel on the 32,768-particle case of this workload (dram__bytes_read
+    # + dram__bytes_write: 3.80 MB for 11.97M particle-days), scaled by the
+    # particle-days of a full launch
+    traffic = 0.318 * pdays
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (scaled from ncu)",
             "peak_source": "measured in this run (FP64 FMA chains; MEASURED_PEAKS.json has no FP64 figure)",
@@ -354,7 +355,8 @@ def main():
                        "parallelism": "dp%d (independent batches, no collective)" % world},
             "gpu_launches": args.steps, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "ias15": {"steps_accepted": stats_acc["steps_accepted"] // args.steps,
+            "ias15": {"kernel_ms_per_step": stats_acc["kernel_ms"] / args.steps,
+                      "steps_accepted": stats_acc["steps_accepted"] // args.steps,
                       "steps_rejected": stats_acc["steps_rejected"] // args.steps,
                       "force_evals": stats_acc["force_evals"] // args.steps,
                       "iterations_per_step": stats_acc["pc_iterations"] / max(stats_acc["steps_accepted"] +

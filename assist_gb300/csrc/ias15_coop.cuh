@@ -76,10 +76,20 @@ __device__ __forceinline__ double ag_colcomp_pos_vfma(const DevEphem& E, const d
     return u;
 }
 
+/* A body table of one substep time and, per body, the origin minus the body's
+ * position: the particle-independent half of every separation
+ * x + (xo - x_body) (src/forces.c), formed once per table rather than once
+ * per particle.  Rows 0..10 planets, then the asteroids. */
+struct AgCoopTab {
+    AgTable T;
+    double rel[AG_NPL + AG_MAX_AST][3];
+};
+
 /* Table pass 1: column and asteroid component sums.  Returns this thread's
  * coverage status (combined by the caller's barrier). */
 __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const ForceCfg& c, double t, AgCoopScratch& S,
-                                                   AgTable& T, int tid) {
+                                                   AgCoopTab& CT, int tid) {
+    AgTable& T = CT.T;
     int bad = 0;
     if (E.pl_spk) {
         /* planets from an SPK file: one thread of warp 1 per body, full state
@@ -90,6 +100,7 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
             if (ag_spk_planet(E, b, t, o) != AG_OK) bad = 1;
             T.P.x[b] = o[1]; T.P.y[b] = o[2]; T.P.z[b] = o[3];
             T.P.vx[b] = o[4]; T.P.vy[b] = o[5]; T.P.vz[b] = o[6];
+            if (c.geocentric != 1) { CT.rel[b][0] = 0.0 - o[1]; CT.rel[b][1] = 0.0 - o[2]; CT.rel[b][2] = 0.0 - o[3]; }
             if (b == AG_EAR && c.geocentric == 1) { T.P.ex_a[0] = o[7]; T.P.ex_a[1] = o[8]; T.P.ex_a[2] = o[9]; }
         }
     } else if (tid < 64) {
@@ -125,15 +136,19 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
 /* Table pass 2: bodies in AU (Earth and Moon from the Earth-Moon barycentre),
  * the Sun's velocity, barycentric asteroids, further EIH velocities and the
  * geocentric Earth acceleration. */
-__device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const ForceCfg& c, double t, AgTable& T,
+__device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const ForceCfg& c, double t, AgCoopTab& CT,
                                                     const AgCoopScratch& S, int tid) {
+    AgTable& T = CT.T;
+    const bool bary = c.geocentric != 1;     /* origin at zero: rel = 0 - x_body */
     if (E.pl_spk) {
         /* planets are in place: only the barycentric asteroids */
         if (tid >= 64)
             for (int q = tid - 64; q < 3 * E.n_ast; q += 64) {
                 const int comp = q % 3;
                 const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
-                T.ast[q / 3][comp] = __dadd_rn(S.ast_h[q / 3][comp], sun);
+                const double xa = __dadd_rn(S.ast_h[q / 3][comp], sun);
+                T.ast[q / 3][comp] = xa;
+                if (bary) CT.rel[AG_NPL + q / 3][comp] = 0.0 - xa;
             }
         return;
     }
@@ -145,6 +160,7 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
         else u = S.col[ag_col_of(b)][comp];
         const double x = __ddiv_rn(u, E.pl_cau);
         if (comp == 0) T.P.x[b] = x; else if (comp == 1) T.P.y[b] = x; else T.P.z[b] = x;
+        if (bary) CT.rel[b][comp] = 0.0 - x;
     } else if (tid < 36) {
         const int comp = tid - 33;
         const double v = __ddiv_rn(S.sun_v[comp], E.cau_per_day);
@@ -153,7 +169,9 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
         for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
             const int comp = task % 3;
             const double sun = __ddiv_rn(S.col[AG_C_SUN][comp], E.pl_cau);
-            T.ast[task / 3][comp] = __dadd_rn(S.ast_h[task / 3][comp], sun);
+            const double xa = __dadd_rn(S.ast_h[task / 3][comp], sun);
+            T.ast[task / 3][comp] = xa;
+            if (bary) CT.rel[AG_NPL + task / 3][comp] = 0.0 - xa;
         }
         int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
         if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
@@ -164,6 +182,48 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
             if (ag_planet_record(E, t, &rec, &tf) == AG_OK) ag_table_velocity(E, rec, tf, j, T);
         }
         if (c.geocentric == 1 && tid == 127) ag_table_earth_acc(E, t, T);
+    }
+}
+
+/* Geocentric origin: rel = x_Earth - x_body, after pass 2 (the caller
+ * synchronises the block before and after). */
+__device__ __forceinline__ void ag_coop_rel_geo(const DevEphem& E, AgCoopTab& CT, int tid) {
+    const PlanetState& P = CT.T.P;
+    for (int q = tid; q < 3 * (AG_NPL + E.n_ast); q += 128) {
+        const int k = q / 3, comp = q % 3;
+        const double xo = comp == 0 ? P.x[AG_EAR] : (comp == 1 ? P.y[AG_EAR] : P.z[AG_EAR]);
+        const double xb = k < AG_NPL ? (comp == 0 ? P.x[k] : (comp == 1 ? P.y[k] : P.z[k])) : CT.T.ast[k - AG_NPL][comp];
+        CT.rel[k][comp] = xo - xb;
+    }
+}
+
+/* Separation of the particle at x from body row k and its inverse length. */
+__device__ __forceinline__ void ag_coop_sep(const AgCoopTab& CT, const double* x, int k, double& dx, double& dy,
+                                            double& dz, double& ri) {
+    dx = x[0] + CT.rel[k][0];
+    dy = x[1] + CT.rel[k][1];
+    dz = x[2] + CT.rel[k][2];
+    ri = rsqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+}
+
+/* Direct gravity of asteroids m0..m1-1 (src/forces.c, the asteroid loop of
+ * the direct term), separations from the table's rel rows. */
+template <bool JAC>
+__device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoopTab& CT, bool on_ast, const double* x,
+                                                  int m0, int m1, double& ax, double& ay, double& az, double (*J)[6]) {
+#pragma unroll 1
+    for (int m = m0; m < m1; m++) {
+        const double ddx = x[0] + CT.rel[AG_NPL + m][0], ddy = x[1] + CT.rel[AG_NPL + m][1],
+                     ddz = x[2] + CT.rel[AG_NPL + m][2];
+        const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
+        const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
+        if (on_ast) { ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az); }
+        if (JAC) {
+            const double g5 = 3.0 * gr3 * rinv * rinv;
+            const double d[3] = {ddx, ddy, ddz};
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
+        }
     }
 }
 
@@ -195,9 +255,10 @@ __device__ __forceinline__ void ag_coop_eih_sources(const DevEphem& E, const For
 /* Warp w's share of the force evaluation at (x, v): partial acceleration and,
  * with JAC, partial 3x6 Jacobian. */
 template <bool JAC>
-__device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const DevEphem& E, const ForceCfg& c,
+__device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, const DevEphem& E, const ForceCfg& c,
                                                   const double* x, const double* v, const double* A, double* acc,
                                                   double (*J)[6]) {
+    const AgTable& T = CT.T;
     const TableBodies B(T);
     const PlanetState& P = T.P;
     double xo[3], vo[3], ao[3];
@@ -211,7 +272,7 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const
     if (w == 0) {
         double dx[AG_NPL], dy[AG_NPL], dz[AG_NPL], ri[AG_NPL];
 #pragma unroll
-        for (int k = 0; k < AG_NPL; k++) ag_sep(P, x, xo, k, dx[k], dy[k], dz[k], ri[k]);
+        for (int k = 0; k < AG_NPL; k++) ag_coop_sep(CT, x, k, dx[k], dy[k], dz[k], ri[k]);
         if ((c.forces & AG_F_NONGRAV) && A != nullptr && (A[0] != 0.0 || A[1] != 0.0 || A[2] != 0.0)) {
             const double d[3] = {dx[AG_SUN], dy[AG_SUN], dz[AG_SUN]};
             const double dv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
@@ -232,12 +293,12 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const
         if (c.forces & AG_F_EIH) {
             double dx[AG_NPL], dy[AG_NPL], dz[AG_NPL], ri[AG_NPL];
 #pragma unroll
-            for (int k = 0; k < AG_NPL; k++) ag_sep(P, x, xo, k, dx[k], dy[k], dz[k], ri[k]);
+            for (int k = 0; k < AG_NPL; k++) ag_coop_sep(CT, x, k, dx[k], dy[k], dz[k], ri[k]);
             ag_term_eih<TableBodies, JAC>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, J);
         }
         if (c.forces & (AG_F_GR_POT | AG_F_GR_SIMPLE)) {
             double p[3], ri;
-            ag_sep(P, x, xo, AG_SUN, p[0], p[1], p[2], ri);
+            ag_coop_sep(CT, x, AG_SUN, p[0], p[1], p[2], ri);
             if (c.forces & AG_F_GR_POT) ag_term_gr_pot<JAC>(E, p, ri, ax, ay, az, J);
             if (c.forces & AG_F_GR_SIMPLE) {
                 const double pv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
@@ -248,16 +309,15 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgTable& T, const
         const bool on_ast = (c.forces & AG_F_AST) != 0;
         const int h = (E.n_ast + 1) / 2;
         if (direct && (on_ast || JAC))
-            st = ag_term_asteroids<TableBodies, JAC>(B, E, on_ast, x, xo, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay,
-                                                     az, J);
+            ag_coop_asteroids<JAC>(E, CT, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay, az, J);
         if (JAC && w == 2 && (c.forces & AG_F_EARTH_H)) {
             double dx, dy, dz, ri;
-            ag_sep(P, x, xo, AG_EAR, dx, dy, dz, ri);
+            ag_coop_sep(CT, x, AG_EAR, dx, dy, dz, ri);
             ag_term_earth_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
         }
         if (w == 3 && (c.forces & AG_F_SUN_H)) {
             double dx, dy, dz, ri;
-            ag_sep(P, x, xo, AG_SUN, dx, dy, dz, ri);
+            ag_coop_sep(CT, x, AG_SUN, dx, dy, dz, ri);
             ag_term_sun_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
         }
     }
@@ -275,9 +335,10 @@ struct AgCoopSeps {
 
 /* The no-Jacobian force share of warps 0 and 1 with the separations split
  * (every lane of both warps calls it; `active` lanes compute). */
-__device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoopSeps& SH, int lane, const AgTable& T,
+__device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoopSeps& SH, int lane, const AgCoopTab& CT,
                                                       const DevEphem& E, const ForceCfg& c, const double* x,
                                                       const double* v, const double* A, double* acc) {
+    const AgTable& T = CT.T;
     const TableBodies B(T);
     const PlanetState& P = T.P;
     double xo[3], vo[3], ao[3];
@@ -287,7 +348,7 @@ __device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoop
     if (active)
         for (int k = k0; k < k1; k++) {
             double dx, dy, dz, ri;
-            ag_sep(P, x, xo, k, dx, dy, dz, ri);
+            ag_coop_sep(CT, x, k, dx, dy, dz, ri);
             SH.d[k][0][lane] = dx; SH.d[k][1][lane] = dy; SH.d[k][2][lane] = dz; SH.ri[k][lane] = ri;
         }
     __syncwarp();
@@ -376,7 +437,7 @@ __device__ __forceinline__ int ag_coop_pcomp(int w) {
 template <int NV>
 struct AgCoopShared {
     static constexpr int C = 3 * (1 + NV);
-    AgTable tab[NV == 0 ? 8 : 1];   /* body tables; without Jacobians one per node, kept through the
+    AgCoopTab tab[NV == 0 ? 8 : 1]; /* body tables; without Jacobians one per node, kept through the
                                        predictor-corrector iterations of a step (the node times do
                                        not change while it iterates) */
     AgCoopScratch scr;
@@ -491,7 +552,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     const DevEphem& E = *Ep;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     __shared__ AgCoopShared<NV> S;
-    AgTable& Tab = S.tab[0];
+    AgCoopTab& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
     extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
     constexpr bool wss = AgCoopDyn<NV, WARM>::ws_shared;
@@ -500,7 +561,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
     const long long clk0 = clock64();
     unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
     if (tid == 0) {
-        for (int k = 0; k < (NV == 0 ? 8 : 1); k++) S.tab[k].status = AG_OK;
+        for (int k = 0; k < (NV == 0 ? 8 : 1); k++) S.tab[k].T.status = AG_OK;
         S.stop = 0;
     }
     /* learned warm start and step logging (no variational particles) */
@@ -623,7 +684,8 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
             ag_coop_table_pass2(E, cf, t, Tab, S.scr, tid);
             __syncthreads();
-            if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab, lane);
+            if (cf.geocentric == 1) { ag_coop_rel_geo(E, Tab, tid); __syncthreads(); }
+            if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, Tab.T, lane);
             int fst = AG_OK;
             {
                 const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};
@@ -674,7 +736,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
             /* ---- learned warm start: features, BF16 inference, b += kappa y */
             bool w_applied = false, w_probe = false;
             if (warm || logp)
-                ag_coop_warm_start(A, W.w, W.ns, W.slot, WS, Tab, lane, wid, live, warm, wl_on, hstep, dtls, steps,
+                ag_coop_warm_start(A, W.w, W.ns, W.slot, WS, Tab.T, lane, wid, live, warm, wl_on, hstep, dtls, steps,
                                    w_applied, w_probe, n_wused, n_wfall);
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
@@ -700,7 +762,7 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                 for (int n = 1; n < 8; n++) {
                     const double hn = ag_ias.h[n];
                     const double tn = t + (tc + hstep * hn);
-                    AgTable& TabN = S.tab[NV == 0 ? n : 0];
+                    AgCoopTab& TabN = S.tab[NV == 0 ? n : 0];
                     const bool build = NV != 0 || iters == 1;     /* block-uniform */
                     bad = build ? ag_coop_table_pass1(E, cf, tn, S.scr, TabN, tid) : 0;
                     if (!conv) {
@@ -732,7 +794,8 @@ __global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep
                     if (build) {
                         ag_coop_table_pass2(E, cf, tn, TabN, S.scr, tid);
                         __syncthreads();
-                        if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, TabN, lane);
+                        if (cf.geocentric == 1) { ag_coop_rel_geo(E, TabN, tid); __syncthreads(); }
+                        if (wid == 1 && (cf.forces & AG_F_EIH)) ag_coop_eih_sources(E, cf, TabN.T, lane);
                     }
                     {
                         const double xp[3] = {S.xs[0][lane], S.xs[1][lane], S.xs[2][lane]};

@@ -581,7 +581,12 @@ struct BatchScratch {
     double* d_ws = nullptr;
     size_t ws_cap = 0;
     int order_cap = 0;
+    float* d_ratio = nullptr;       /* pilot: encounter cost ratio per particle */
+    int ratio_cap = 0;
+    float4* d_grid = nullptr;       /* pilot: body positions on the time grid */
+    float2* d_sunv = nullptr;
 };
+#define AG_PILOT_G 1024
 static std::mutex g_batch_mu;
 static BatchScratch g_batch;
 
@@ -756,6 +761,35 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             has_ng[(size_t)i] = prm[3 * (size_t)i] != 0.0 || prm[3 * (size_t)i + 1] != 0.0 || prm[3 * (size_t)i + 2] != 0.0;
     }
     if (ag_cuda_check(cudaStreamSynchronize(s), "read inputs")) return ASSIST_ERROR_EPHEM_FILE;
+    /* close-encounter pilot (queue order of the groups only) */
+    std::vector<float> enc;
+    if (grouped) {
+        double tmin = t0[0], tmax = t0[0];
+        for (int i = 0; i < n; i++) {
+            tmin = std::min(tmin, std::min(t0[(size_t)i], te[(size_t)i]));
+            tmax = std::max(tmax, std::max(t0[(size_t)i], te[(size_t)i]));
+        }
+        if (g_batch.ratio_cap < n) {
+            if (g_batch.d_ratio) cudaFree(g_batch.d_ratio);
+            g_batch.d_ratio = nullptr;
+            g_batch.ratio_cap = 0;
+            if (ag_cuda_check(cudaMalloc(&g_batch.d_ratio, sizeof(float) * (size_t)n), "cudaMalloc(pilot)"))
+                return ASSIST_ERROR_EPHEM_FILE;
+            g_batch.ratio_cap = n;
+        }
+        if (!g_batch.d_grid &&
+            (ag_cuda_check(cudaMalloc(&g_batch.d_grid, sizeof(float4) * AG_PILOT_G * 10), "cudaMalloc(pilot grid)") ||
+             ag_cuda_check(cudaMalloc(&g_batch.d_sunv, sizeof(float2) * AG_PILOT_G), "cudaMalloc(pilot grid)")))
+            return ASSIST_ERROR_EPHEM_FILE;
+        enc.resize((size_t)n);
+        if (ag_cuda_check((cudaError_t)ag_pilot_encounters(D, n, d_t0, d_t_end, d_state, tmin, tmax, g_batch.d_ratio,
+                                                           g_batch.d_grid, g_batch.d_sunv, AG_PILOT_G, s),
+                          "pilot kernels") ||
+            ag_cuda_check(cudaMemcpyAsync(enc.data(), g_batch.d_ratio, sizeof(float) * n, cudaMemcpyDeviceToHost, s),
+                          "read pilot") ||
+            ag_cuda_check(cudaStreamSynchronize(s), "read pilot"))
+            return ASSIST_ERROR_EPHEM_FILE;
+    }
     std::vector<int> order((size_t)n), gstart, gsize;
     for (int i = 0; i < n; i++) order[(size_t)i] = i;
     if (!grouped) {
@@ -808,7 +842,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
                     ((unsigned)(bucket + (1 << 28)) & ((1u << 30) - 1));
             k.idx = i;
             k.neg_len = -L;
-            k.cost = L * std::pow(q, -0.6);
+            k.cost = L * std::pow(q, -0.6) * (1.0 + (double)enc[(size_t)i]);
         }
         });
         ag_parallel_sort(key);
@@ -836,7 +870,8 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         /* most expensive group first: a particle's evaluations grow with its
          * length and shrink with perihelion distance, about L q^-0.6 (fitted
          * to per-particle IAS15 evaluation counts of a main-belt/NEO/Trojan/TNO
-         * mixture) */
+         * mixture), times 1 + the pilot's encounter ratio; a group costs its
+         * most expensive member */
         std::vector<int> gi(gstart.size());
         for (size_t k = 0; k < gi.size(); k++) gi[k] = (int)k;
         std::stable_sort(gi.begin(), gi.end(), [&](int a, int b) { return gl[(size_t)a] > gl[(size_t)b]; });

@@ -95,6 +95,8 @@ clib.assist_gb300_forces_device.argtypes = [c_void_p, POINTER(Options), c_int, c
 clib.assist_gb300_forces_device.restype = c_int
 clib.assist_gb300_ephem_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_ephem_device.restype = c_int
+clib.assist_gb300_encounter_ratio_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+clib.assist_gb300_encounter_ratio_device.restype = c_int
 clib.assist_gb300_n_bodies.argtypes = [c_void_p]
 clib.assist_gb300_n_bodies.restype = c_int
 clib.assist_gb300_last_error.restype = c_char_p

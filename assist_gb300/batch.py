@@ -144,6 +144,21 @@ def bodies_device(ephem: Ephem, t, out=None, status=None, stream=None):
     return out
 
 
+def encounter_ratio_device(ephem: Ephem, t0, t_end, state, out=None, stream=None):
+    """Close-encounter cost ratio per particle (torch CUDA float32): the IAS15
+    steps close planetary encounters add over [t0, t_end], as a fraction of
+    the particle's plain steps (the estimate the grouped kernels queue by)."""
+    import torch
+    n = state.shape[0]
+    if out is None:
+        out = torch.empty(n, dtype=torch.float32, device=state.device)
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_encounter_ratio_device(byref(ephem), n, _ptr(t0), _ptr(t_end), _ptr(state), _ptr(out), s)
+    if rc != 0:
+        raise RuntimeError("assist_gb300_encounter_ratio_device failed (%d): %s" % (rc, last_error()))
+    return out
+
+
 def fp64_peak_gflops() -> float:
     """Measured FP64 FMA throughput of the current device (GFLOP/s)."""
     return float(clib.assist_gb300_fp64_peak_gflops())

@@ -1013,3 +1013,38 @@ extern "C" int assist_gb300_integrate_batch(const struct assist_ephem* e, const 
 
 /* FP64 FMA throughput of the current device in GFLOP/s (roofline denominator). */
 extern "C" double assist_gb300_fp64_peak_gflops(void) { return ag_fp64_probe_gflops(); }
+
+extern "C" int assist_gb300_encounter_ratio_device(const struct assist_ephem* e, int n, const double* d_t0,
+                                                   const double* d_t_end, const double* d_state, float* d_ratio,
+                                                   void* stream) {
+    if (n < 0 || (n > 0 && (!d_t0 || !d_t_end || !d_state || !d_ratio))) {
+        ag_set_error("encounter ratio: n must be >= 0 and every array given");
+        return ASSIST_ERROR_N;
+    }
+    if (n == 0) return ASSIST_SUCCESS;
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<double> t0((size_t)n), te((size_t)n);
+    if (ag_cuda_check(cudaMemcpyAsync(t0.data(), d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
+        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end") ||
+        ag_cuda_check(cudaStreamSynchronize(s), "read times"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    double tmin = t0[0], tmax = t0[0];
+    for (int i = 0; i < n; i++) {
+        tmin = std::min(tmin, std::min(t0[(size_t)i], te[(size_t)i]));
+        tmax = std::max(tmax, std::max(t0[(size_t)i], te[(size_t)i]));
+    }
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    if (!g_batch.d_grid &&
+        (ag_cuda_check(cudaMalloc(&g_batch.d_grid, sizeof(float4) * AG_PILOT_G * 10), "cudaMalloc(pilot grid)") ||
+         ag_cuda_check(cudaMalloc(&g_batch.d_sunv, sizeof(float2) * AG_PILOT_G), "cudaMalloc(pilot grid)")))
+        return ASSIST_ERROR_EPHEM_FILE;
+    if (ag_cuda_check((cudaError_t)ag_pilot_encounters(D, n, d_t0, d_t_end, d_state, tmin, tmax, d_ratio,
+                                                       g_batch.d_grid, g_batch.d_sunv, AG_PILOT_G, s),
+                      "pilot kernels") ||
+        ag_cuda_check(cudaStreamSynchronize(s), "pilot kernels"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    return ASSIST_SUCCESS;
+}

@@ -349,6 +349,16 @@ int assist_gb300_forces_device(const struct assist_ephem* ephem, const struct as
 int assist_gb300_ephem_device(const struct assist_ephem* ephem, int n, const double* d_t,
                               double* d_out, int* d_status, void* stream);
 
+/* Close-encounter cost ratio of each particle: the IAS15 steps its close
+ * planetary encounters add over [t0, t_end], as a fraction of its plain
+ * steps, from the two-body pilot by which the grouped batched kernels order
+ * their work queue (FP32 estimate; device arrays, d_ratio receives n floats).
+ * No counterpart in the reference: a scheduling aid, e.g. to shard particles
+ * across GPUs by expected cost. */
+int assist_gb300_encounter_ratio_device(const struct assist_ephem* ephem, int n, const double* d_t0,
+                                        const double* d_t_end, const double* d_state, float* d_ratio,
+                                        void* stream);
+
 /* FP64 fused multiply-add throughput of the current CUDA device in GFLOP/s,
  * measured with independent FMA chains (the roofline denominator of these
  * FP64-bound kernels). */

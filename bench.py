@@ -353,7 +353,9 @@ def main():
                                      "beside it under learned_warm_start)",
                        "l2": "flushed (256 MB write) between steps", "kernel": "block-cooperative groups (group_steps=2)",
                        "parallelism": "dp%d (independent batches, no collective)" % world},
-            "gpu_launches": 3 * args.steps,   # per step: the encounter pilot's two kernels and the IAS15 kernel "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            # per step: the encounter pilot's two kernels and the IAS15 kernel
+            "gpu_launches": 3 * args.steps,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "ias15": {"kernel_ms_per_step": stats_acc["kernel_ms"] / args.steps,
                       "steps_accepted": stats_acc["steps_accepted"] // args.steps,

@@ -667,19 +667,20 @@ static void ag_parallel_for(int n, const F& f) {
 }
 
 /* Sort key of one particle for grouping: start time, then class (direction,
- * non-gravitational parameters, timescale bucket), then length (longest
- * first), then index, a strict total order (the result does not depend on the
- * sort algorithm). */
+ * non-gravitational parameters, timescale bucket), then the two keys within
+ * a class, then index: a strict total order (the result does not depend on
+ * the sort algorithm). */
 struct AgGroupKey {
     double t0;
     unsigned cls;
     int idx;
-    double neg_len;
-    double cost;            /* expected evaluations, L q^-0.6 */
+    double k1, k2;          /* within a class: ascending */
+    double cost;            /* expected evaluations, L q^-0.6 (1 + encounter ratio) */
     bool operator<(const AgGroupKey& b) const {
         if (t0 != b.t0) return t0 < b.t0;
         if (cls != b.cls) return cls < b.cls;
-        if (neg_len != b.neg_len) return neg_len < b.neg_len;
+        if (k1 != b.k1) return k1 < b.k1;
+        if (k2 != b.k2) return k2 < b.k2;
         return idx < b.idx;
     }
 };
@@ -800,8 +801,9 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
     } else {
         /* groups share t0, direction and whether non-gravitational
          * parameters are present; within them particles of similar orbital
-         * timescale (perihelion distance q^1.5, quarter-octave bins) and
-         * similar length sit together; groups are queued longest first */
+         * timescale (perihelion distance q^1.5, eighth-octave bins), similar
+         * length and similar time of pericentre passage sit together; groups
+         * are queued most expensive first */
         const double gm = (e->ascii_planets || e->spk_planets) ? ag_sun_gm(e) : 2.9591220828411951e-04;
         std::vector<AgGroupKey> key((size_t)n);
         ag_parallel_for(n, [&](int i0, int i1) {
@@ -816,7 +818,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             const double inv_a = 2.0 / r - v2 / gm;
             double q = (std::fabs(inv_a) > 1e-12) ? (1.0 - ecc) / inv_a : r;
             if (!(q > 1e-4)) q = 1e-4;
-            int bucket = (int)std::floor(4.0 * std::log2(std::pow(q, 1.5)));
+            int bucket = (int)std::floor(8.0 * std::log2(std::pow(q, 1.5)));
             if (o->group_order == 1) {
                 /* orbit size (half octaves of a; unbound orbits last), length
                  * (factors of 2), then mean anomaly in 1/64 turns */
@@ -841,7 +843,27 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             k.cls = ((te[(size_t)i] >= t0[(size_t)i]) ? 0u : (1u << 31)) | (has_ng[(size_t)i] ? (1u << 30) : 0u) |
                     ((unsigned)(bucket + (1 << 28)) & ((1u << 30) - 1));
             k.idx = i;
-            k.neg_len = -L;
+            if (o->group_order == 1) {
+                k.k1 = -L;
+                k.k2 = 0.0;
+            } else {
+                /* within a bucket: lengths in sixteenths of an octave (longest
+                 * first: a group's lanes end within 4.4 % of each other), then
+                 * the time to the next pericentre passage (the last one for
+                 * backward integrations), so that the members of a group
+                 * reach their smallest steps together */
+                double tp = 0.0;
+                if (inv_a > 1e-12 && ecc < 1.0 && ecc > 1e-9) {
+                    const double a = 1.0 / inv_a;
+                    const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
+                    double M = std::atan2(se, ce) - se;                  /* e sin E = se */
+                    M = M - 2.0 * M_PI * std::floor(M / (2.0 * M_PI));
+                    const double nm = std::sqrt(gm * inv_a * inv_a * inv_a);
+                    tp = (te[(size_t)i] >= t0[(size_t)i]) ? (2.0 * M_PI - M) / nm : M / nm;
+                }
+                k.k1 = -std::floor(16.0 * std::log2(std::max(L, 1e-3)));
+                k.k2 = tp;
+            }
             k.cost = L * std::pow(q, -0.6) * (1.0 + (double)enc[(size_t)i]);
         }
         });

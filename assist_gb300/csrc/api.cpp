@@ -585,6 +585,10 @@ struct BatchScratch {
     int ratio_cap = 0;
     float4* d_grid = nullptr;       /* pilot: body positions on the time grid */
     float2* d_sunv = nullptr;
+    double* h_in = nullptr;         /* pinned: t0, t_end, states, parameters read back for grouping */
+    size_t h_in_cap = 0;
+    float* h_ratio = nullptr;       /* pinned: the pilot's ratios */
+    int h_ratio_cap = 0;
 };
 #define AG_PILOT_G 1024
 static std::mutex g_batch_mu;
@@ -741,29 +745,42 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         while (tpb > 32 && (n + tpb - 1) / tpb < sms) tpb /= 2;
     }
-    std::vector<double> t0((size_t)n), te((size_t)n), st0;
-    if (ag_cuda_check(cudaMemcpyAsync(t0.data(), d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
-        ag_cuda_check(cudaMemcpyAsync(te.data(), d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end"))
-        return ASSIST_ERROR_EPHEM_FILE;
-    if (grouped) {
-        st0.resize(6 * (size_t)n);
-        if (ag_cuda_check(cudaMemcpyAsync(st0.data(), d_state, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, s), "read state"))
+    /* inputs read back for grouping, through pinned staging (kept between calls) */
+    const size_t need_in = (size_t)n * (grouped ? 11 : 2);
+    if (g_batch.h_in_cap < need_in) {
+        if (g_batch.h_in) cudaFreeHost(g_batch.h_in);
+        g_batch.h_in = nullptr;
+        g_batch.h_in_cap = 0;
+        if (ag_cuda_check(cudaMallocHost(&g_batch.h_in, sizeof(double) * need_in), "cudaMallocHost(inputs)"))
             return ASSIST_ERROR_EPHEM_FILE;
+        g_batch.h_in_cap = need_in;
     }
+    double* const t0 = g_batch.h_in;
+    double* const te = t0 + n;
+    double* const st0 = te + n;                       /* grouped only: 6n states, then 3n parameters */
+    double* const prm = st0 + 6 * (size_t)n;
+    if (ag_cuda_check(cudaMemcpyAsync(t0, d_t0, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t0") ||
+        ag_cuda_check(cudaMemcpyAsync(te, d_t_end, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "read t_end"))
+        return ASSIST_ERROR_EPHEM_FILE;
     /* particles with non-gravitational parameters are grouped apart: a
      * group pays for the term when any member has it */
-    std::vector<unsigned char> has_ng((size_t)n, 0);
-    if (grouped && d_params && (c.forces & AG_F_NONGRAV)) {
-        std::vector<double> prm(3 * (size_t)n);
-        if (ag_cuda_check(cudaMemcpyAsync(prm.data(), d_params, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "read params"))
+    const bool read_prm = grouped && d_params && (c.forces & AG_F_NONGRAV);
+    if (grouped) {
+        if (ag_cuda_check(cudaMemcpyAsync(st0, d_state, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, s), "read state"))
             return ASSIST_ERROR_EPHEM_FILE;
-        if (ag_cuda_check(cudaStreamSynchronize(s), "read params")) return ASSIST_ERROR_EPHEM_FILE;
-        for (int i = 0; i < n; i++)
-            has_ng[(size_t)i] = prm[3 * (size_t)i] != 0.0 || prm[3 * (size_t)i + 1] != 0.0 || prm[3 * (size_t)i + 2] != 0.0;
+        if (read_prm &&
+            ag_cuda_check(cudaMemcpyAsync(prm, d_params, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "read params"))
+            return ASSIST_ERROR_EPHEM_FILE;
     }
     if (ag_cuda_check(cudaStreamSynchronize(s), "read inputs")) return ASSIST_ERROR_EPHEM_FILE;
-    /* close-encounter pilot (queue order of the groups only) */
-    std::vector<float> enc;
+    std::vector<unsigned char> has_ng((size_t)n, 0);
+    if (read_prm)
+        for (int i = 0; i < n; i++)
+            has_ng[(size_t)i] = prm[3 * (size_t)i] != 0.0 || prm[3 * (size_t)i + 1] != 0.0 || prm[3 * (size_t)i + 2] != 0.0;
+    /* close-encounter pilot (queue order of the groups only): it runs on the
+     * device while the host sorts the batch; its ratios are read before the
+     * group costs are formed */
+    const float* enc = nullptr;
     if (grouped) {
         double tmin = t0[0], tmax = t0[0];
         for (int i = 0; i < n; i++) {
@@ -772,9 +789,12 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         }
         if (g_batch.ratio_cap < n) {
             if (g_batch.d_ratio) cudaFree(g_batch.d_ratio);
+            if (g_batch.h_ratio) cudaFreeHost(g_batch.h_ratio);
             g_batch.d_ratio = nullptr;
+            g_batch.h_ratio = nullptr;
             g_batch.ratio_cap = 0;
-            if (ag_cuda_check(cudaMalloc(&g_batch.d_ratio, sizeof(float) * (size_t)n), "cudaMalloc(pilot)"))
+            if (ag_cuda_check(cudaMalloc(&g_batch.d_ratio, sizeof(float) * (size_t)n), "cudaMalloc(pilot)") ||
+                ag_cuda_check(cudaMallocHost(&g_batch.h_ratio, sizeof(float) * (size_t)n), "cudaMallocHost(pilot)"))
                 return ASSIST_ERROR_EPHEM_FILE;
             g_batch.ratio_cap = n;
         }
@@ -782,14 +802,13 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             (ag_cuda_check(cudaMalloc(&g_batch.d_grid, sizeof(float4) * AG_PILOT_G * 10), "cudaMalloc(pilot grid)") ||
              ag_cuda_check(cudaMalloc(&g_batch.d_sunv, sizeof(float2) * AG_PILOT_G), "cudaMalloc(pilot grid)")))
             return ASSIST_ERROR_EPHEM_FILE;
-        enc.resize((size_t)n);
         if (ag_cuda_check((cudaError_t)ag_pilot_encounters(D, n, d_t0, d_t_end, d_state, tmin, tmax, g_batch.d_ratio,
                                                            g_batch.d_grid, g_batch.d_sunv, AG_PILOT_G, s),
                           "pilot kernels") ||
-            ag_cuda_check(cudaMemcpyAsync(enc.data(), g_batch.d_ratio, sizeof(float) * n, cudaMemcpyDeviceToHost, s),
-                          "read pilot") ||
-            ag_cuda_check(cudaStreamSynchronize(s), "read pilot"))
+            ag_cuda_check(cudaMemcpyAsync(g_batch.h_ratio, g_batch.d_ratio, sizeof(float) * n, cudaMemcpyDeviceToHost, s),
+                          "read pilot"))
             return ASSIST_ERROR_EPHEM_FILE;
+        enc = g_batch.h_ratio;
     }
     std::vector<int> order((size_t)n), gstart, gsize;
     for (int i = 0; i < n; i++) order[(size_t)i] = i;
@@ -864,11 +883,13 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
                 k.k1 = -std::floor(16.0 * std::log2(std::max(L, 1e-3)));
                 k.k2 = tp;
             }
-            k.cost = L * std::pow(q, -0.6) * (1.0 + (double)enc[(size_t)i]);
+            k.cost = L * std::pow(q, -0.6);
         }
         });
         ag_parallel_sort(key);
         for (int i = 0; i < n; i++) order[(size_t)i] = key[(size_t)i].idx;
+        if (ag_cuda_check(cudaStreamSynchronize(s), "pilot kernels")) return ASSIST_ERROR_EPHEM_FILE;
+        for (int i = 0; i < n; i++) key[(size_t)i].cost *= 1.0 + (double)enc[key[(size_t)i].idx];
         /* group_order 1 orders by its bucket but breaks groups only at start
          * time, direction and the non-gravitational flag */
         const unsigned brk = o->group_order == 0 ? ~0u : (3u << 30);

@@ -547,7 +547,11 @@ struct AgCoopDyn {
 };
 
 template <int NV, bool WARM>
-__global__ void __launch_bounds__(128) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
+/* Three blocks per SM for the plain kernel (168 registers, a few spills:
+ * 1.5 % faster than two at 236); the variational and warm-start
+ * instantiations keep two (their Jacobians or network buffers would spill or
+ * not fit). */
+__global__ void __launch_bounds__(128, (NV == 0 && !WARM) ? 3 : 2) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
     const DevEphem& E = *Ep;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;

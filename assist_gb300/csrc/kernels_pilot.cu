@@ -111,19 +111,23 @@ __global__ void ag_k_pilot(const DevEphem* __restrict__ Ep, int n, const double*
     float gmk[AG_PILOT_NB];
     for (int b = 1; b < AG_PILOT_NB; b++) gmk[b] = (float)E.gm[ag_pilot_body[b]];
     float base = 0.0f, extra = 0.0f;
+    /* mean anomaly at the first sample in FP64, then FP32 increments (the
+     * loop stays off the FP64 pipe) */
     const double twopi = 6.283185307179586;
+    double Ms = M0 + nmot * ((tmin + dtg * i0) - ta);
+    Ms -= twopi * floor(Ms / twopi);
+    const float Mstart = (float)Ms, dM = (float)(nmot * dtg), tpf = 6.2831853f, itpf = 1.0f / 6.2831853f;
     for (int q = i0; q <= i1; q++) {
-        double M = M0 + nmot * ((tmin + dtg * q) - ta);
-        M -= twopi * floor(M / twopi);
-        const float Mf = (float)M;
-        float Ea = Mf + fe * sinf(Mf);
+        float Mf = fmaf((float)(q - i0), dM, Mstart);
+        Mf -= tpf * floorf(Mf * itpf);
+        float Ea = Mf + fe * __sinf(Mf);
         for (int it = 0; it < 6; it++) {
             float sE, cE;
-            sincosf(Ea, &sE, &cE);
+            __sincosf(Ea, &sE, &cE);
             Ea -= (Ea - fe * sE - Mf) / (1.0f - fe * cE);
         }
         float sE, cE;
-        sincosf(Ea, &sE, &cE);
+        __sincosf(Ea, &sE, &cE);
         const float xo = fa * (cE - fe), yo = fb * sE;
         const float px = xo * Pf[0] + yo * Qf[0], py = xo * Pf[1] + yo * Qf[1], pz = xo * Pf[2] + yo * Qf[2];
         const float r2 = px * px + py * py + pz * pz;

@@ -45,7 +45,7 @@ class Options(ctypes.Structure):
                 ("alpha", c_double), ("nk", c_double), ("nm", c_double), ("nn", c_double), ("r0", c_double),
                 ("epsilon", c_double), ("min_dt", c_double), ("dt0", c_double), ("max_steps", c_int),
                 ("warm_start", c_int), ("threads_per_block", c_int), ("group_steps", c_int),
-                ("dt_floor", c_double), ("group_order", c_int)]
+                ("dt_floor", c_double), ("group_order", c_int), ("blocks_per_sm", c_int)]
 
 
 class BatchStats(ctypes.Structure):
@@ -97,6 +97,9 @@ clib.assist_gb300_ephem_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, 
 clib.assist_gb300_ephem_device.restype = c_int
 clib.assist_gb300_encounter_ratio_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_encounter_ratio_device.restype = c_int
+clib.assist_gb300_group_plan.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_double,
+                                         c_void_p, c_void_p, c_void_p, POINTER(c_int)]
+clib.assist_gb300_group_plan.restype = c_int
 clib.assist_gb300_n_bodies.argtypes = [c_void_p]
 clib.assist_gb300_n_bodies.restype = c_int
 clib.assist_gb300_last_error.restype = c_char_p

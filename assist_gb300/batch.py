@@ -7,7 +7,7 @@ torch CUDA tensors (torch is used only for device memory and streams).
 """
 from __future__ import annotations
 
-from ctypes import byref, c_void_p
+from ctypes import byref, c_int, c_void_p
 from typing import Optional
 
 import numpy as np
@@ -157,6 +157,27 @@ def encounter_ratio_device(ephem: Ephem, t0, t_end, state, out=None, stream=None
     if rc != 0:
         raise RuntimeError("assist_gb300_encounter_ratio_device failed (%d): %s" % (rc, last_error()))
     return out
+
+
+def group_plan(t0, t_end, state, params=None, ratio=None, group_order: int = 0,
+               gm_sun: float = 2.9591220828411951e-04):
+    """The grouped kernels' grouping on host arrays: (order, groups) with
+    groups a list of index arrays into the batch, most expensive first."""
+    t0 = np.ascontiguousarray(t0, np.float64)
+    n = t0.shape[0]
+    te = np.ascontiguousarray(t_end, np.float64)
+    st = np.ascontiguousarray(state, np.float64).reshape(n, 6)
+    prm = None if params is None else np.ascontiguousarray(params, np.float64).reshape(n, 3)
+    rat = None if ratio is None else np.ascontiguousarray(ratio, np.float32).reshape(n)
+    order = np.empty(n, np.int32); gs = np.empty(max(n, 1), np.int32); gz = np.empty(max(n, 1), np.int32)
+    ng = c_int(0)
+    rc = clib.assist_gb300_group_plan(n, t0.ctypes.data, te.ctypes.data, st.ctypes.data,
+                                      None if prm is None else prm.ctypes.data,
+                                      None if rat is None else rat.ctypes.data, group_order, gm_sun,
+                                      order.ctypes.data, gs.ctypes.data, gz.ctypes.data, byref(ng))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_group_plan failed (%d): %s" % (rc, last_error()))
+    return order, [order[s:s + z] for s, z in zip(gs[:ng.value], gz[:ng.value])]
 
 
 def fp64_peak_gflops() -> float:

@@ -542,6 +542,7 @@ extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
     o->group_steps = 2;
     o->dt_floor = 1e-8;
     o->group_order = 0;
+    o->blocks_per_sm = 0;
 }
 
 extern "C" int assist_gb300_n_bodies(const struct assist_ephem* e) { return ag_ephem_n_bodies(e); }
@@ -713,6 +714,151 @@ static void ag_parallel_sort(std::vector<AgGroupKey>& v) {
     }
 }
 
+/* Sort keys of a batch for grouping (host arrays): class, the keys within
+ * a class and the base cost of every particle, sorted.  has_ng may be NULL. */
+static void ag_group_keys(int n, const double* t0, const double* te, const double* st0, const unsigned char* has_ng,
+                          double gm, int group_order, std::vector<AgGroupKey>& key) {
+    /* groups share t0, direction and whether non-gravitational
+     * parameters are present; within them particles of similar orbital
+     * timescale (perihelion distance q^1.5, eighth-octave bins), similar
+     * length and similar time of pericentre passage sit together; groups
+     * are queued most expensive first */
+    key.assign((size_t)n, AgGroupKey{});
+    ag_parallel_for(n, [&](int i0, int i1) {
+    for (int i = i0; i < i1; i++) {
+        const double* p = &st0[6 * (size_t)i];
+        const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        const double v2 = p[3] * p[3] + p[4] * p[4] + p[5] * p[5];
+        const double rv = p[0] * p[3] + p[1] * p[4] + p[2] * p[5];
+        double ev[3];
+        for (int k = 0; k < 3; k++) ev[k] = ((v2 - gm / r) * p[k] - rv * p[3 + k]) / gm;
+        const double ecc = std::sqrt(ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
+        const double inv_a = 2.0 / r - v2 / gm;
+        double q = (std::fabs(inv_a) > 1e-12) ? (1.0 - ecc) / inv_a : r;
+        if (!(q > 1e-4)) q = 1e-4;
+        int bucket = (int)std::floor(8.0 * std::log2(std::pow(q, 1.5)));
+        if (group_order == 1) {
+            /* orbit size (half octaves of a; unbound orbits last), length
+             * (factors of 2), then mean anomaly in 1/64 turns */
+            const double L = std::fabs(te[(size_t)i] - t0[(size_t)i]);
+            int ba = 1000, bm = 0;
+            if (inv_a > 1e-12 && ecc < 1.0) {
+                const double a = 1.0 / inv_a;
+                ba = (int)std::floor(2.0 * std::log2(a));
+                const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
+                const double E = std::atan2(se, ce);
+                double M = E - se;                      /* e sin E = se */
+                M = M - 2.0 * M_PI * std::floor(M / (2.0 * M_PI));
+                bm = (int)std::floor(64.0 * M / (2.0 * M_PI));
+            }
+            const int bl = (int)std::floor(std::log2(std::max(L, 1e-3)));
+            bucket = ((ba + 2000) * 64 + (bl + 32)) * 64 + bm;
+        }
+        /* class bits: 31 backward, 30 non-gravitational, 0..29 bucket */
+        const double L = std::fabs(te[(size_t)i] - t0[(size_t)i]);
+        AgGroupKey& k = key[(size_t)i];
+        k.t0 = t0[(size_t)i];
+        k.cls = ((te[(size_t)i] >= t0[(size_t)i]) ? 0u : (1u << 31)) | ((has_ng && has_ng[(size_t)i]) ? (1u << 30) : 0u) |
+                ((unsigned)(bucket + (1 << 28)) & ((1u << 30) - 1));
+        k.idx = i;
+        if (group_order == 1) {
+            k.k1 = -L;
+            k.k2 = 0.0;
+        } else {
+            /* within a bucket: lengths in sixteenths of an octave (longest
+             * first: a group's lanes end within 4.4 % of each other), then
+             * the time to the next pericentre passage (the last one for
+             * backward integrations), so that the members of a group
+             * reach their smallest steps together */
+            double tp = 0.0;
+            if (inv_a > 1e-12 && ecc < 1.0 && ecc > 1e-9) {
+                const double a = 1.0 / inv_a;
+                const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
+                double M = std::atan2(se, ce) - se;                  /* e sin E = se */
+                M = M - 2.0 * M_PI * std::floor(M / (2.0 * M_PI));
+                const double nm = std::sqrt(gm * inv_a * inv_a * inv_a);
+                tp = (te[(size_t)i] >= t0[(size_t)i]) ? (2.0 * M_PI - M) / nm : M / nm;
+            }
+            k.k1 = -std::floor(16.0 * std::log2(std::max(L, 1e-3)));
+            k.k2 = tp;
+            if (inv_a > 1e-12 && ecc < 1.0 && ecc > 1e-9 && tp > L) {
+                /* an interval shorter than half an orbit without a pericentre
+                 * passage: its smallest heliocentric distance, at one of its
+                 * ends, sets the steps rather than q; bucket by it and order
+                 * by that end */
+                const double a = 1.0 / inv_a;
+                const double nm = std::sqrt(gm * inv_a * inv_a * inv_a);
+                if (L * nm < M_PI) {
+                    const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
+                    double M = std::atan2(se, ce) - se;
+                    double M1 = M + ((te[(size_t)i] >= t0[(size_t)i]) ? nm * L : -nm * L);
+                    M1 = M1 - 2.0 * M_PI * std::floor(M1 / (2.0 * M_PI));
+                    double E1 = M1 + ecc * std::sin(M1);
+                    for (int it = 0; it < 30; it++) {
+                        const double dE = (E1 - ecc * std::sin(E1) - M1) / (1.0 - ecc * std::cos(E1));
+                        E1 -= dE;
+                        if (std::fabs(dE) < 1e-12) break;
+                    }
+                    const double r1 = a * (1.0 - ecc * std::cos(E1));
+                    const double rmin = std::min(r, r1);
+                    k.k2 = (r1 < r) ? L : 0.0;
+                    const int b2 = (int)std::floor(8.0 * std::log2(std::pow(std::max(rmin, 1e-4), 1.5)));
+                    k.cls = (k.cls & (3u << 30)) | ((unsigned)(b2 + (1 << 28)) & ((1u << 30) - 1));
+                }
+            }
+        }
+        k.cost = L * std::pow(q, -0.6);
+    }
+    });
+    ag_parallel_sort(key);
+}
+
+/* Groups of 32 from the sorted keys, most expensive first: order receives
+ * the particles in key order, gstart/gsize the groups in queue order.  ratio
+ * (the encounter pilot's output, per particle) may be NULL. */
+static void ag_group_form(std::vector<AgGroupKey>& key, const float* ratio, int group_order, std::vector<int>& order,
+                          std::vector<int>& gstart, std::vector<int>& gsize) {
+    const int n = (int)key.size();
+    order.resize((size_t)n);
+    gstart.clear();
+    gsize.clear();
+    for (int i = 0; i < n; i++) order[(size_t)i] = key[(size_t)i].idx;
+    if (ratio)
+        for (int i = 0; i < n; i++) key[(size_t)i].cost *= 1.0 + (double)ratio[key[(size_t)i].idx];
+    /* group_order 1 orders by its bucket but breaks groups only at start
+     * time, direction and the non-gravitational flag */
+    const unsigned brk = group_order == 0 ? ~0u : (3u << 30);
+    std::vector<double> gl;
+    int i = 0;
+    while (i < n) {
+        const AgGroupKey& a = key[(size_t)i];
+        double m = a.cost;
+        int j = i + 1;
+        while (j < n && j - i < 32) {
+            const AgGroupKey& b = key[(size_t)j];
+            if (b.t0 != a.t0 || ((b.cls ^ a.cls) & brk)) break;
+            m = std::max(m, b.cost);
+            j++;
+        }
+        gstart.push_back(i);
+        gsize.push_back(j - i);
+        gl.push_back(m);
+        i = j;
+    }
+    /* most expensive group first: a particle's evaluations grow with its
+     * length and shrink with perihelion distance, about L q^-0.6 (fitted
+     * to per-particle IAS15 evaluation counts of a main-belt/NEO/Trojan/TNO
+     * mixture), times 1 + the pilot's encounter ratio; a group costs its
+     * most expensive member */
+    std::vector<int> gi(gstart.size());
+    for (size_t k = 0; k < gi.size(); k++) gi[k] = (int)k;
+    std::stable_sort(gi.begin(), gi.end(), [&](int a, int b) { return gl[(size_t)a] > gl[(size_t)b]; });
+    std::vector<int> s2(gi.size()), z2(gi.size());
+    for (size_t k = 0; k < gi.size(); k++) { s2[k] = gstart[(size_t)gi[k]]; z2[k] = gsize[(size_t)gi[k]]; }
+    gstart.swap(s2);
+    gsize.swap(z2);
+}
+
 static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
                               const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
                               int n_var, double* d_var_state, int* d_status, void* stream,
@@ -818,116 +964,30 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             return std::fabs(te[(size_t)a] - t0[(size_t)a]) > std::fabs(te[(size_t)b] - t0[(size_t)b]);
         });
     } else {
-        /* groups share t0, direction and whether non-gravitational
-         * parameters are present; within them particles of similar orbital
-         * timescale (perihelion distance q^1.5, eighth-octave bins), similar
-         * length and similar time of pericentre passage sit together; groups
-         * are queued most expensive first */
         const double gm = (e->ascii_planets || e->spk_planets) ? ag_sun_gm(e) : 2.9591220828411951e-04;
-        std::vector<AgGroupKey> key((size_t)n);
-        ag_parallel_for(n, [&](int i0, int i1) {
-        for (int i = i0; i < i1; i++) {
-            const double* p = &st0[6 * (size_t)i];
-            const double r = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-            const double v2 = p[3] * p[3] + p[4] * p[4] + p[5] * p[5];
-            const double rv = p[0] * p[3] + p[1] * p[4] + p[2] * p[5];
-            double ev[3];
-            for (int k = 0; k < 3; k++) ev[k] = ((v2 - gm / r) * p[k] - rv * p[3 + k]) / gm;
-            const double ecc = std::sqrt(ev[0] * ev[0] + ev[1] * ev[1] + ev[2] * ev[2]);
-            const double inv_a = 2.0 / r - v2 / gm;
-            double q = (std::fabs(inv_a) > 1e-12) ? (1.0 - ecc) / inv_a : r;
-            if (!(q > 1e-4)) q = 1e-4;
-            int bucket = (int)std::floor(8.0 * std::log2(std::pow(q, 1.5)));
-            if (o->group_order == 1) {
-                /* orbit size (half octaves of a; unbound orbits last), length
-                 * (factors of 2), then mean anomaly in 1/64 turns */
-                const double L = std::fabs(te[(size_t)i] - t0[(size_t)i]);
-                int ba = 1000, bm = 0;
-                if (inv_a > 1e-12 && ecc < 1.0) {
-                    const double a = 1.0 / inv_a;
-                    ba = (int)std::floor(2.0 * std::log2(a));
-                    const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
-                    const double E = std::atan2(se, ce);
-                    double M = E - se;                      /* e sin E = se */
-                    M = M - 2.0 * M_PI * std::floor(M / (2.0 * M_PI));
-                    bm = (int)std::floor(64.0 * M / (2.0 * M_PI));
-                }
-                const int bl = (int)std::floor(std::log2(std::max(L, 1e-3)));
-                bucket = ((ba + 2000) * 64 + (bl + 32)) * 64 + bm;
-            }
-            /* class bits: 31 backward, 30 non-gravitational, 0..29 bucket */
-            const double L = std::fabs(te[(size_t)i] - t0[(size_t)i]);
-            AgGroupKey& k = key[(size_t)i];
-            k.t0 = t0[(size_t)i];
-            k.cls = ((te[(size_t)i] >= t0[(size_t)i]) ? 0u : (1u << 31)) | (has_ng[(size_t)i] ? (1u << 30) : 0u) |
-                    ((unsigned)(bucket + (1 << 28)) & ((1u << 30) - 1));
-            k.idx = i;
-            if (o->group_order == 1) {
-                k.k1 = -L;
-                k.k2 = 0.0;
-            } else {
-                /* within a bucket: lengths in sixteenths of an octave (longest
-                 * first: a group's lanes end within 4.4 % of each other), then
-                 * the time to the next pericentre passage (the last one for
-                 * backward integrations), so that the members of a group
-                 * reach their smallest steps together */
-                double tp = 0.0;
-                if (inv_a > 1e-12 && ecc < 1.0 && ecc > 1e-9) {
-                    const double a = 1.0 / inv_a;
-                    const double ce = (1.0 - r * inv_a), se = rv / std::sqrt(gm * a);
-                    double M = std::atan2(se, ce) - se;                  /* e sin E = se */
-                    M = M - 2.0 * M_PI * std::floor(M / (2.0 * M_PI));
-                    const double nm = std::sqrt(gm * inv_a * inv_a * inv_a);
-                    tp = (te[(size_t)i] >= t0[(size_t)i]) ? (2.0 * M_PI - M) / nm : M / nm;
-                }
-                k.k1 = -std::floor(16.0 * std::log2(std::max(L, 1e-3)));
-                k.k2 = tp;
-            }
-            k.cost = L * std::pow(q, -0.6);
-        }
-        });
-        ag_parallel_sort(key);
-        for (int i = 0; i < n; i++) order[(size_t)i] = key[(size_t)i].idx;
+        std::vector<AgGroupKey> key;
+        ag_group_keys(n, t0, te, st0, has_ng.data(), gm, o->group_order, key);
         if (ag_cuda_check(cudaStreamSynchronize(s), "pilot kernels")) return ASSIST_ERROR_EPHEM_FILE;
-        for (int i = 0; i < n; i++) key[(size_t)i].cost *= 1.0 + (double)enc[key[(size_t)i].idx];
-        /* group_order 1 orders by its bucket but breaks groups only at start
-         * time, direction and the non-gravitational flag */
-        const unsigned brk = o->group_order == 0 ? ~0u : (3u << 30);
-        std::vector<double> gl;
-        int i = 0;
-        while (i < n) {
-            const AgGroupKey& a = key[(size_t)i];
-            double m = a.cost;
-            int j = i + 1;
-            while (j < n && j - i < 32) {
-                const AgGroupKey& b = key[(size_t)j];
-                if (b.t0 != a.t0 || ((b.cls ^ a.cls) & brk)) break;
-                m = std::max(m, b.cost);
-                j++;
-            }
-            gstart.push_back(i);
-            gsize.push_back(j - i);
-            gl.push_back(m);
-            i = j;
-        }
-        /* most expensive group first: a particle's evaluations grow with its
-         * length and shrink with perihelion distance, about L q^-0.6 (fitted
-         * to per-particle IAS15 evaluation counts of a main-belt/NEO/Trojan/TNO
-         * mixture), times 1 + the pilot's encounter ratio; a group costs its
-         * most expensive member */
-        std::vector<int> gi(gstart.size());
-        for (size_t k = 0; k < gi.size(); k++) gi[k] = (int)k;
-        std::stable_sort(gi.begin(), gi.end(), [&](int a, int b) { return gl[(size_t)a] > gl[(size_t)b]; });
-        std::vector<int> s2(gi.size()), z2(gi.size());
-        for (size_t k = 0; k < gi.size(); k++) { s2[k] = gstart[(size_t)gi[k]]; z2[k] = gsize[(size_t)gi[k]]; }
-        gstart.swap(s2);
-        gsize.swap(z2);
+        ag_group_form(key, enc, o->group_order, order, gstart, gsize);
     }
-    int nslots;
+    int nslots, occ = 2;
     const bool coop = o->group_steps == 2;
     if (coop) {
         /* one 32-particle group per 128-thread block */
-        nslots = ag_coop_max_slots(n_var);
+        /* three resident blocks per SM (the plain kernel's 168-register
+         * build) when the batch has at least 8 groups per such block: the
+         * throughput gain outweighs the slower longest groups; two otherwise */
+        if (n_var == 0 && !o->warm_start) {
+            if (o->blocks_per_sm == 2 || o->blocks_per_sm == 3) {
+                occ = o->blocks_per_sm;
+            } else {
+                int dev = 0, sms = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                occ = (int)gstart.size() >= 8 * 3 * sms ? 3 : 2;
+            }
+        }
+        nslots = ag_coop_max_slots(n_var, occ);
         const int need = 32 * (int)gstart.size();
         if (nslots > need) nslots = need;
     } else if (grouped) {
@@ -995,7 +1055,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int le = coop ? ag_launch_coop(D, c, a, n_var, s)
+    int le = coop ? ag_launch_coop(D, c, a, n_var, occ, s)
                   : (grouped ? ag_launch_group(D, c, a, n_var, s) : ag_launch_batch(D, c, a, n_var, tpb, s));
     cudaEventRecord(e1, s);
     if (le) { cudaEventDestroy(e0); cudaEventDestroy(e1); ag_cuda_check((cudaError_t)le, "batch kernel launch"); return ASSIST_ERROR_EPHEM_FILE; }
@@ -1089,5 +1149,30 @@ extern "C" int assist_gb300_encounter_ratio_device(const struct assist_ephem* e,
                       "pilot kernels") ||
         ag_cuda_check(cudaStreamSynchronize(s), "pilot kernels"))
         return ASSIST_ERROR_EPHEM_FILE;
+    return ASSIST_SUCCESS;
+}
+
+extern "C" int assist_gb300_group_plan(int n, const double* t0, const double* t_end, const double* state,
+                                       const double* params, const float* ratio, int group_order, double gm_sun,
+                                       int* order, int* gstart, int* gsize, int* n_groups) {
+    if (n < 0 || (n > 0 && (!t0 || !t_end || !state || !order || !gstart || !gsize || !n_groups)) ||
+        (group_order != 0 && group_order != 1) || !(gm_sun > 0.0)) {
+        ag_set_error("group plan: n >= 0, every output array, group_order 0 or 1 and gm_sun > 0 are required");
+        return ASSIST_ERROR_N;
+    }
+    if (n_groups) *n_groups = 0;
+    if (n == 0) return ASSIST_SUCCESS;
+    std::vector<unsigned char> has_ng((size_t)n, 0);
+    if (params)
+        for (int i = 0; i < n; i++)
+            has_ng[(size_t)i] = params[3 * (size_t)i] != 0.0 || params[3 * (size_t)i + 1] != 0.0 || params[3 * (size_t)i + 2] != 0.0;
+    std::vector<AgGroupKey> key;
+    ag_group_keys(n, t0, t_end, state, has_ng.data(), gm_sun, group_order, key);
+    std::vector<int> ord, gs, gz;
+    ag_group_form(key, ratio, group_order, ord, gs, gz);
+    std::copy(ord.begin(), ord.end(), order);
+    std::copy(gs.begin(), gs.end(), gstart);
+    std::copy(gz.begin(), gz.end(), gsize);
+    *n_groups = (int)gs.size();
     return ASSIST_SUCCESS;
 }

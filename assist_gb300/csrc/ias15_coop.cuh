@@ -546,12 +546,14 @@ struct AgCoopDyn {
     static constexpr size_t bytes = warm + ws;
 };
 
-template <int NV, bool WARM>
-/* Three blocks per SM for the plain kernel (168 registers, a few spills:
- * 1.5 % faster than two at 236); the variational and warm-start
- * instantiations keep two (their Jacobians or network buffers would spill or
- * not fit). */
-__global__ void __launch_bounds__(128, (NV == 0 && !WARM) ? 3 : 2) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
+/* OCC: resident blocks per SM the kernel is compiled for.  The plain kernel
+ * comes in two builds: 2 (236 registers) and 3 (168 registers, a few
+ * spills: 1.5 % faster on batches with many groups per block, slower on
+ * small batches whose longest groups set the time); the variational and
+ * warm-start instantiations have only 2 (their Jacobians or network buffers
+ * would spill or not fit). */
+template <int NV, bool WARM, int OCC = 2>
+__global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
     const DevEphem& E = *Ep;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -1064,38 +1066,46 @@ __global__ void __launch_bounds__(128, (NV == 0 && !WARM) ? 3 : 2) ag_k_coop(con
 }
 
 /* Opt the kernel in to its dynamic shared memory (above the 48 KB default). */
-template <int NV, bool WARM>
+template <int NV, bool WARM, int OCC>
 static int ag_coop_dyn_attr() {
     if (AgCoopDyn<NV, WARM>::bytes == 0) return 0;
-    return (int)cudaFuncSetAttribute(ag_k_coop<NV, WARM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return (int)cudaFuncSetAttribute(ag_k_coop<NV, WARM, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)AgCoopDyn<NV, WARM>::bytes);
 }
 
-int ag_coop_max_slots(int nv) {
+/* Slots (32 per resident block) of the plain (nv = 0, occ 2 or 3) or
+ * variational (nv = 6) kernel on the current device. */
+int ag_coop_max_slots(int nv, int occ) {
     int dev = 0, sms = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (nv == 6) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false>, 128, AgCoopDyn<6, false>::bytes);
-    } else if (ag_coop_dyn_attr<0, false>() == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false>, 128, AgCoopDyn<0, false>::bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false, 2>, 128, AgCoopDyn<6, false>::bytes);
+    } else if (occ == 3) {
+        if (ag_coop_dyn_attr<0, false, 3>() == 0)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false, 3>, 128, AgCoopDyn<0, false>::bytes);
+    } else if (ag_coop_dyn_attr<0, false, 2>() == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false, 2>, 128, AgCoopDyn<0, false>::bytes);
     }
     if (bps < 1) bps = 1;
     return sms * bps * 32;
 }
 
-int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s) {
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, cudaStream_t s) {
     int e = ag_ias_tables_init();
     if (e) return e;
     const int blocks = (a.nslots + 31) / 32;
     if (nv == 6) {
-        ag_k_coop<6, false><<<blocks, 128, AgCoopDyn<6, false>::bytes, s>>>(E.self_dev, c, a);
+        ag_k_coop<6, false, 2><<<blocks, 128, AgCoopDyn<6, false>::bytes, s>>>(E.self_dev, c, a);
     } else if (a.mlp || a.log_x) {
-        if ((e = ag_coop_dyn_attr<0, true>())) return e;
-        ag_k_coop<0, true><<<blocks, 128, AgCoopDyn<0, true>::bytes, s>>>(E.self_dev, c, a);
+        if ((e = ag_coop_dyn_attr<0, true, 2>())) return e;
+        ag_k_coop<0, true, 2><<<blocks, 128, AgCoopDyn<0, true>::bytes, s>>>(E.self_dev, c, a);
+    } else if (occ == 3) {
+        if ((e = ag_coop_dyn_attr<0, false, 3>())) return e;
+        ag_k_coop<0, false, 3><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
     } else {
-        if ((e = ag_coop_dyn_attr<0, false>())) return e;
-        ag_k_coop<0, false><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
+        if ((e = ag_coop_dyn_attr<0, false, 2>())) return e;
+        ag_k_coop<0, false, 2><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
     }
     return (int)cudaGetLastError();
 }

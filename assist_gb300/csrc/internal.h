@@ -71,13 +71,13 @@ int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, 
 int ag_batch_max_slots(int nv, int tpb);
 int ag_group_max_slots(int nv);
 int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
-int ag_coop_max_slots(int nv);
+int ag_coop_max_slots(int nv, int occ);
 /* Per-particle encounter cost ratio (extra steps / base steps) from a
  * two-body pilot on a G-point time grid over [tmin, tmax]. */
 int ag_pilot_encounters(const DevEphem& E, int n, const double* d_t0, const double* d_te, const double* d_state,
                         double tmin, double tmax, float* d_ratio, float4* d_grid, float2* d_sunv, int G,
                         cudaStream_t s);
-int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, cudaStream_t s);
 double ag_fp64_probe_gflops(void);
 
 /* shared-step device IAS15 (kernels_shared.cu) */

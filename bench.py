@@ -217,6 +217,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="plain predictor only (no learned warm start)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0,
+                    help="block-cooperative kernel residency: 0 automatic (the library's choice), 2 or 3")
     ap.add_argument("--particles", type=int, default=None, help="override the batch size (profiling only)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -244,7 +246,7 @@ def main():
     prm = torch.tensor(pop.params, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
-    opts = batch.options(group_steps=2, warm_start=0)
+    opts = batch.options(group_steps=2, warm_start=0, blocks_per_sm=args.blocks_per_sm)
     warm_opts = batch.options(group_steps=2, warm_start=1)
     warm_info = None
     if not args.no_warm:

@@ -213,7 +213,11 @@ struct assist_gb300_options {
                                stops with ASSIST_GB300_STEP_UNDERFLOW (an impact: any orbit
                                outside a body needs steps > 1e-4 day); 0 disables */
     int group_order;        /* how groups are formed (group_steps 1, 2): 0 (default) perihelion
-                               distance then length; 1 orbit size, length, then mean anomaly */
+                               distance, length, then time of pericentre passage; 1 orbit size,
+                               length, then mean anomaly */
+    int blocks_per_sm;      /* group_steps 2 without variational particles or warm start:
+                               0 (default) three resident blocks per SM when the batch has at
+                               least 8 groups per such block, else two; 2 or 3 force it */
 };
 
 /* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */
@@ -358,6 +362,16 @@ int assist_gb300_ephem_device(const struct assist_ephem* ephem, int n, const dou
 int assist_gb300_encounter_ratio_device(const struct assist_ephem* ephem, int n, const double* d_t0,
                                         const double* d_t_end, const double* d_state, float* d_ratio,
                                         void* stream);
+
+/* The grouping of the grouped batched kernels, on host arrays and without
+ * device work: order[n] receives the particles in key order, gstart[] and
+ * gsize[] (room for n each) the groups of at most 32 consecutive entries of
+ * order, most expensive first, *n_groups their count.  params (3 doubles per
+ * particle) and ratio (the encounter pilot's output, n floats) may be NULL;
+ * gm_sun is the Sun's GM in AU^3/day^2.  No counterpart in the reference. */
+int assist_gb300_group_plan(int n, const double* t0, const double* t_end, const double* state, const double* params,
+                            const float* ratio, int group_order, double gm_sun, int* order, int* gstart, int* gsize,
+                            int* n_groups);
 
 /* FP64 fused multiply-add throughput of the current CUDA device in GFLOP/s,
  * measured with independent FMA chains (the roofline denominator of these

@@ -336,11 +336,11 @@ def main():
     kernel_s = stats_acc["kernel_ms"] / 1e3
     peak = batch.fp64_peak_gflops() * 1e9
     achieved = flops / kernel_s
-    # DRAM bytes per launch: 0.318 B per particle-day, from one ncu capture of
-    # this kernel on the 32,768-particle case of this workload (dram__bytes_read
-    # + dram__bytes_write: 3.80 MB for 11.97M particle-days), scaled by the
-    # particle-days of a full launch
-    traffic = 0.318 * pdays
+    # DRAM bytes per launch: 0.351 B per particle-day, from one ncu capture of
+    # this kernel (three-blocks-per-SM build) on the 32,768-particle case of
+    # this workload (dram__bytes_read + dram__bytes_write: 4.20 MB for 11.97M
+    # particle-days), scaled by the particle-days of a full launch
+    traffic = 0.351 * pdays
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (scaled from ncu)",
             "peak_source": "measured in this run (FP64 FMA chains; MEASURED_PEAKS.json has no FP64 figure)",

@@ -919,6 +919,11 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
             return ASSIST_ERROR_EPHEM_FILE;
     }
     if (ag_cuda_check(cudaStreamSynchronize(s), "read inputs")) return ASSIST_ERROR_EPHEM_FILE;
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(t0[(size_t)i]) || !std::isfinite(te[(size_t)i])) {
+            ag_set_error("t0 and t_end must be finite (particle " + std::to_string(i) + ")");
+            return ASSIST_ERROR_N;
+        }
     std::vector<unsigned char> has_ng((size_t)n, 0);
     if (read_prm)
         for (int i = 0; i < n; i++)
@@ -1162,6 +1167,11 @@ extern "C" int assist_gb300_group_plan(int n, const double* t0, const double* t_
     }
     if (n_groups) *n_groups = 0;
     if (n == 0) return ASSIST_SUCCESS;
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(t0[i]) || !std::isfinite(t_end[i])) {
+            ag_set_error("group plan: t0 and t_end must be finite");
+            return ASSIST_ERROR_N;
+        }
     std::vector<unsigned char> has_ng((size_t)n, 0);
     if (params)
         for (int i = 0; i < n; i++)

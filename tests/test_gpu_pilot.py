@@ -68,3 +68,16 @@ def test_queue_order_does_not_change_results(synth_files):
     ok = (sa == 0) & (sc == 0)
     assert ok.mean() > 0.99
     assert np.abs(a[ok, :3] - c[ok, :3]).max() < 1e-9
+
+
+def test_batch_rejects_non_finite_times(synth_files):
+    """A NaN or infinite start or end time is an argument error, not a
+    particle status (the grouping sorts by time)."""
+    from assist_gb300 import Ephem, batch, synth
+    pl, ast, system = synth_files
+    eph = Ephem(pl, ast)
+    pop = synth.population(system, "mix", 64, seed=3, t0=8000.0, length=30.0)
+    for bad in (np.nan, np.inf):
+        te = pop.t_end.copy(); te[5] = bad
+        with pytest.raises(RuntimeError):
+            batch.integrate_batch(eph, pop.t0, te, pop.state, opts=batch.options(group_steps=2))

@@ -114,3 +114,6 @@ def test_group_plan_rejects_bad_arguments():
         batch.group_plan(t0, te, st, group_order=7)
     order, groups = batch.group_plan(t0[:0], te[:0], st[:0])
     assert order.size == 0 and groups == []
+    bad = t0.copy(); bad[3] = np.nan
+    with pytest.raises(RuntimeError):
+        batch.group_plan(bad, te, st)

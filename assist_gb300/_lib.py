@@ -1,7 +1,7 @@
 """Loader for libassist_gb300.so (mirrors assist/_libassist.py of ASSIST).
 
-The library is built in place by ``assist_gb300.build`` (or
-``__graft_entry__.build()``).  Set ASSIST_GB300_LIB to force a specific file.
+The library is built in place by ``python assist_gb300/build.py`` (a script:
+importing the package needs the library) or ``__graft_entry__.build()``.  Set ASSIST_GB300_LIB to force a specific file.
 There is no CPU fallback: a missing library is an ImportError.
 """
 from __future__ import annotations
@@ -13,7 +13,7 @@ from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_longlong, c_ul
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.environ.get("ASSIST_GB300_LIB", os.path.join(HERE, "libassist_gb300.so"))
 if not os.path.exists(LIBPATH):
-    raise ImportError("libassist_gb300.so not found at %s: run `python -m assist_gb300.build` "
+    raise ImportError("libassist_gb300.so not found at %s: run `python assist_gb300/build.py` "
                       "(or __graft_entry__.build()) first" % LIBPATH)
 clib = ctypes.CDLL(LIBPATH)
 __libpath__ = LIBPATH

@@ -19,7 +19,8 @@ from .ephem import Ephem
 def options(**kw) -> Options:
     """ASSIST's defaults (src/assist.c:408-447) overridden by keyword arguments:
     forces, gr_eih_sources, geocentric, alpha, nk, nm, nn, r0, epsilon, min_dt,
-    dt0, max_steps, warm_start, threads_per_block."""
+    dt0, max_steps, warm_start, threads_per_block, group_steps, dt_floor,
+    group_order, blocks_per_sm (struct assist_gb300_options in assist.h)."""
     o = Options()
     clib.assist_gb300_default_options(byref(o))
     for k, v in kw.items():

@@ -39,6 +39,15 @@
  * Per evaluation this cuts the FP64 instructions on one sub-partition to
  * roughly a third of the warp-grouped kernel's, which is what bounds the
  * longest groups (the tail of a batch).
+ *
+ * Memory: without variational particles the block keeps the eight node
+ * tables of a step (the node times do not change while the predictor-
+ * corrector iterates, so each table is built once per step), each with the
+ * origin-minus-body half of every separation formed once, and the group's
+ * IAS15 state (40 fields x 3 components x 32 lanes) in dynamic shared
+ * memory.  The plain kernel is built for two resident blocks per SM (236
+ * registers) and for three (168); the host picks three only for batches
+ * with many groups per block.
  */
 
 /* Raw sums of one substep time, shared by the block. */

@@ -117,3 +117,23 @@ def test_group_plan_rejects_bad_arguments():
     bad = t0.copy(); bad[3] = np.nan
     with pytest.raises(RuntimeError):
         batch.group_plan(bad, te, st)
+
+
+def test_group_plan_edge_cases():
+    """One particle; zero-length and backward intervals; unbound and
+    non-finite states (finite times) all form valid groups."""
+    from assist_gb300 import batch
+    t0, te, st, prm, k2, dist = _pop(n=200, seed=4)
+    order, groups = batch.group_plan(t0[:1], te[:1], st[:1])
+    assert order.tolist() == [0] and [g.tolist() for g in groups] == [[0]]
+    st2 = st.copy()
+    st2[0, 3:] *= 5.0                       # hyperbolic
+    st2[1] = np.nan                         # non-finite state
+    st2[2, :3] = 0.0                        # at the origin
+    te2 = te.copy(); te2[3] = t0[3]         # zero length
+    order, groups = batch.group_plan(t0, te2, st2, params=prm)
+    assert sorted(np.concatenate(groups).tolist()) == list(range(200))
+    assert all(1 <= g.size <= 32 for g in groups)
+    # the queue is a permutation of the groups in both group orders
+    order1, groups1 = batch.group_plan(t0, te2, st2, params=prm, group_order=1)
+    assert sorted(np.concatenate(groups1).tolist()) == list(range(200))

@@ -52,7 +52,7 @@ class BatchStats(ctypes.Structure):
     """struct assist_gb300_batch_stats (include/assist.h)."""
     _fields_ = [("steps_accepted", c_longlong), ("steps_rejected", c_longlong), ("force_evals", c_longlong),
                 ("pc_iterations", c_longlong), ("warm_start_used", c_longlong), ("warm_start_fallback", c_longlong),
-                ("kernel_ms", c_double)]
+                ("kernel_ms", c_double), ("tables_built", c_longlong)]
 
 
 clib.assist_gb300_default_options.argtypes = [POINTER(Options)]

@@ -1076,6 +1076,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         stats->pc_iterations = (long long)cnt[3];
         stats->warm_start_used = (long long)cnt[4];
         stats->warm_start_fallback = (long long)cnt[5];
+        stats->tables_built = (long long)cnt[6];
         stats->kernel_ms = ms;
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);

@@ -97,6 +97,20 @@ __device__ __forceinline__ bool ag_isnormal_pos(double a) {
     return a >= 2.2250738585072014e-308 && a <= 1.7976931348623157e308;
 }
 
+/* Sub-interval b of tt = record fraction x niv and the integer part fl with
+ * tau = 2 (tt - fl) - 1, as src/ascii_ephem.c:35-39 takes them: b = (int)tt
+ * and fmod(tt, 1) = tt - trunc(tt) (exact).  A time a rounding below a record
+ * boundary gives a tiny negative tt: b = 0, tau just below -1, the record's
+ * start.  At tt == niv exactly the reference reads one sub-interval past the
+ * column; here b stays in the last sub-interval, at its end (tau = +1). */
+__device__ __forceinline__ int ag_subinterval(double tt, int niv, double* fl) {
+    int b = (int)tt;
+    double f = trunc(tt);
+    if (b >= niv) { b = niv - 1; f = (double)(niv - 1); }
+    *fl = f;
+    return b;
+}
+
 /* Planet record selection shared by all eleven planets at one time
  * (src/ascii_ephem.c:294-300).  Returns AG_OK or AG_ERR_COVERAGE. */
 __device__ __forceinline__ int ag_planet_record(const DevEphem& E, double t, const double** rec, double* tf) {
@@ -118,9 +132,8 @@ __device__ __forceinline__ void ag_column(const DevEphem& E, const double* rec, 
                                           double* u, double* v) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
     const double tt = tf * (double)niv;
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;                 /* tf == 1 exactly: stay in the last sub-interval */
+    double fl;
+    const int b = ag_subinterval(tt, niv, &fl);
     const double tau = 2.0 * (tt - fl) - 1.0;
     const double two_tau = 2.0 * tau;
     const double* P = rec + E.col_off[col] + ncf * 3 * b;
@@ -222,9 +235,8 @@ __device__ __forceinline__ void ag_column_exact(const DevEphem& E, const double*
                                                 double* v) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
     const double tt = __dmul_rn(tf, (double)niv);
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;
+    double fl;
+    const int b = ag_subinterval(tt, niv, &fl);
     const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
     const double two_t0 = __dmul_rn(2.0, t0);
     const double* P = rec + E.col_off[col] + ncf * 3 * b;
@@ -285,9 +297,8 @@ __device__ __forceinline__ void ag_column_pva_exact(const DevEphem& E, const dou
                                                     double* v, double* w) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
     const double tt = __dmul_rn(tf, (double)niv);
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;
+    double fl;
+    const int b = ag_subinterval(tt, niv, &fl);
     const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
     const double two_t0 = __dmul_rn(2.0, t0);
     const double c = __ddiv_rn(__ddiv_rn((double)(niv * 2), E.pl_inc), 86400.0);

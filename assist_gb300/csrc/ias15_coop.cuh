@@ -65,9 +65,8 @@ __device__ __forceinline__ double ag_colcomp_pos_vfma(const DevEphem& E, const d
                                                       double* vsum) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
     const double tt = __dmul_rn(tf, (double)niv);
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;
+    double fl;
+    const int b = ag_subinterval(tt, niv, &fl);
     const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
     const double two_t0 = __dmul_rn(2.0, t0);
     const double* P = rec + E.col_off[col] + ncf * (3 * b + comp);
@@ -574,7 +573,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
     const Ws<C> W{wss ? reinterpret_cast<double*>(ag_dyn_smem + AgCoopDyn<NV, WARM>::warm) : A.ws,
                   wss ? 32 : A.nslots, wss ? lane : slot};
     const long long clk0 = clock64();
-    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0;
+    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_wused = 0, n_wfall = 0, n_tab = 0;
     if (tid == 0) {
         for (int k = 0; k < (NV == 0 ? 8 : 1); k++) S.tab[k].T.status = AG_OK;
         S.stop = 0;
@@ -586,11 +585,23 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
 
     while (true) {
         __syncthreads();
-        if (tid == 0) S.g = S.stop ? A.n_groups : atomicAdd(A.queue, 1);
+        if (tid == 0) S.g = atomicAdd(A.queue, 1);
         __syncthreads();
         const int g = S.g;
         if (g >= A.n_groups) break;
         const int gs = A.grp_size[g], g0 = A.grp_start[g];
+        if (S.stop) {
+            /* run-time budget spent: groups still queued are not integrated
+             * (state untouched) and say so */
+            if (wid == 0 && lane < gs) {
+                const int p = A.order[g0 + lane];
+                if (A.status) A.status[p] = AG_ST_TIMEOUT;
+                if (NV == 0 && A.out_start != nullptr)
+                    for (int q = A.out_start[p]; q < A.out_start[p + 1]; q++)
+                        for (int k = 0; k < 6; k++) A.out_state[6 * (size_t)q + k] = __longlong_as_double(0x7ff8000000000000LL);
+            }
+            continue;
+        }
         const int pid = lane < gs ? A.order[g0 + lane] : -1;
         double t = A.t0[A.order[g0]], tc = 0.0, dtls = 0.0;
         const double tend = pid >= 0 ? A.t_end[pid] : t;
@@ -692,6 +703,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
 
             /* ---- node 0: accelerations at the step start, g from the predicted b */
             int bad = ag_coop_table_pass1(E, cf, t, S.scr, Tab, tid);
+            n_tab++;
             if (live)
                 for (int comp = 0; comp < C; comp++)
                     if (ag_coop_owner<NV>(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
@@ -780,6 +792,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                     AgCoopTab& TabN = S.tab[NV == 0 ? n : 0];
                     const bool build = NV != 0 || iters == 1;     /* block-uniform */
                     bad = build ? ag_coop_table_pass1(E, cf, tn, S.scr, TabN, tid) : 0;
+                    n_tab += build ? 1 : 0;
                     if (!conv) {
                         double sx[9], sv[8];
                         sx[0] = hstep * hn;
@@ -921,9 +934,11 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                 else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
                 dt_new_l = fabs(dn);
             }
-            if (live && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
+            if (live && !last_group && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
                 /* step underflow: this lane's particle is hitting a body; it stops
-                 * (state of the step start) and the group goes on without it */
+                 * (state of the step start) and the group goes on without it.  Not
+                 * tested on a step cut short to land on a member's t_end: the
+                 * proposals scale with that short step */
                 pstat = AG_ST_UNDERFLOW;
                 finish_now = true;
                 rej_l = false;
@@ -1071,6 +1086,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
         atomicAdd(&A.counters[3], n_it);
         atomicAdd(&A.counters[4], n_wused);
         atomicAdd(&A.counters[5], n_wfall);
+        if (tid == 0) atomicAdd(&A.counters[6], n_tab);   /* body tables, one per block and node time */
     }
 }
 

@@ -159,10 +159,16 @@ __global__ void __launch_bounds__(128) ag_k_batch(const DevEphem* __restrict__ E
 
     while (true) {
         if (pid < 0) {
-            if (stop) break;
             const int qpos = atomicAdd(A.queue, 1);
             if (qpos >= A.n) break;
             pid = A.order[qpos];
+            if (stop) {
+                /* run-time budget spent: the particles still queued are not
+                 * integrated (state untouched) and say so */
+                if (A.status) A.status[pid] = AG_ST_TIMEOUT;
+                pid = -1;
+                continue;
+            }
             const double* s0 = A.state + 6 * (size_t)pid;
             for (int k = 0; k < 3; k++) {
                 W(W_X0, k) = s0[k]; W(W_V0, k) = s0[3 + k]; W(W_XC, k) = 0.0; W(W_VC, k) = 0.0;
@@ -331,8 +337,10 @@ __global__ void __launch_bounds__(128) ag_k_batch(const DevEphem* __restrict__ E
                             if (fabs(ratio) < safety) reject = true;
                             else if (fabs(ratio) > 1.0 / safety) dt_new = hstep / safety;
                         }
-                        if (A.dt_floor > 0.0 && fabs(dt_new) < A.dt_floor) {
-                            /* step underflow: the particle is hitting a body */
+                        if (!last && A.dt_floor > 0.0 && fabs(dt_new) < A.dt_floor) {
+                            /* step underflow: the particle is hitting a body (not
+                             * tested on a step cut short to land on t_end, whose
+                             * proposal scales with the short step) */
                             pstat = AG_ST_UNDERFLOW;
                             phase = 3;
                         } else if (reject) {
@@ -415,6 +423,7 @@ __global__ void __launch_bounds__(128) ag_k_batch(const DevEphem* __restrict__ E
     atomicAdd(&A.counters[1], n_rej);
     atomicAdd(&A.counters[2], n_ev);
     atomicAdd(&A.counters[3], n_it);
+    atomicAdd(&A.counters[6], n_ev);     /* every evaluation evaluates its own bodies */
 }
 
 int ag_batch_max_slots(int nv, int tpb) {
@@ -523,15 +532,20 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const Ws<C> W{A.ws, A.nslots, slot};
     const long long clk0 = clock64();
-    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0;
-    bool stop = false;
+    unsigned long long n_acc = 0, n_rej = 0, n_ev = 0, n_it = 0, n_tab = 0;
+    bool stop = false;     /* warp-uniform */
 
-    while (!stop) {
+    while (true) {
         int g = 0;
         if (lane == 0) g = atomicAdd(A.queue, 1);
         g = __shfl_sync(AG_FULL, g, 0);
         if (g >= A.n_groups) break;
         const int gs = A.grp_size[g], g0 = A.grp_start[g];
+        if (stop) {
+            /* run-time budget spent: groups still queued are not integrated */
+            if (lane < gs && A.status) A.status[A.order[g0 + lane]] = AG_ST_TIMEOUT;
+            continue;
+        }
         const int pid = lane < gs ? A.order[g0 + lane] : -1;
         double t = A.t0[A.order[g0]], tc = 0.0, dtls = 0.0;
         const double tend = pid >= 0 ? A.t_end[pid] : t;
@@ -590,7 +604,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
                 finish_now = false;
             }
             if (!__any_sync(AG_FULL, live)) break;
-            if (A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles) {
+            if (__any_sync(AG_FULL, A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles)) {
                 pstat = AG_ST_TIMEOUT;
                 finish_now = live;
                 stop = true;
@@ -606,6 +620,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
             const bool last = live && last_group && rem == rem_min;
             /* ---- node 0: accelerations at the step start, g from the predicted b */
             int st = ag_warp_table_fast(E, cf, t, Tab, Scr, lane);
+            n_tab++;
             if (st != AG_OK) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
             if (live) {
                 double at[C];
@@ -651,6 +666,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
                     const double hn = ag_ias.h[n];
                     const double tn = t + (tc + hstep * hn);
                     st = ag_warp_table_fast(E, cf, tn, Tab, Scr, lane);
+                    n_tab++;
                     if (st != AG_OK) break;
                     if (!conv) {
                         double sx[9], sv[8];
@@ -744,9 +760,11 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
                 else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
                 dt_new_l = fabs(dn);
             }
-            if (live && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
+            if (live && !last_group && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
                 /* step underflow: this lane's particle is hitting a body; it stops
-                 * (state of the step start) and the group goes on without it */
+                 * (state of the step start) and the group goes on without it.  Not
+                 * tested on a step cut short to land on a member's t_end: the
+                 * proposals scale with that short step */
                 pstat = AG_ST_UNDERFLOW;
                 finish_now = true;
                 rej_l = false;
@@ -823,6 +841,7 @@ __global__ void __launch_bounds__(128) ag_k_group(const DevEphem* __restrict__ E
     atomicAdd(&A.counters[1], n_rej);
     atomicAdd(&A.counters[2], n_ev);
     atomicAdd(&A.counters[3], n_it);
+    if (lane == 0) atomicAdd(&A.counters[6], n_tab);   /* body tables, one per warp and node time */
 }
 
 int ag_group_max_slots(int nv) {

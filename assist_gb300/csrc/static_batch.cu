@@ -140,6 +140,7 @@ extern "C" int assist_gb300_integrate_batch_device_static(const struct assist_ep
         stats->pc_iterations = (long long)cnt[3];
         stats->warm_start_used = (long long)cnt[4];
         stats->warm_start_fallback = (long long)cnt[5];
+        stats->tables_built = (long long)cnt[6];
         stats->kernel_ms = -1.0;   /* not timed: timing would need events */
     }
     return ASSIST_SUCCESS;

@@ -30,9 +30,8 @@ __device__ __forceinline__ double ag_colcomp_exact(const DevEphem& E, const doub
                                                    double* vsum) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
     const double tt = __dmul_rn(tf, (double)niv);
-    const double fl = floor(tt);
-    int b = (int)tt;
-    if (b >= niv) b = niv - 1;
+    double fl;
+    const int b = ag_subinterval(tt, niv, &fl);
     const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
     const double two_t0 = __dmul_rn(2.0, t0);
     const double* P = rec + E.col_off[col] + ncf * (3 * b + comp);

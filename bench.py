@@ -15,24 +15,35 @@ One step = one pass of the hot path over the whole batch: every particle
 integrated from t0 to its t_end by the persistent kernel.
 
   value : particle-days/s of the default path (plain IAS15 predictor) with
-          inputs resident in HBM, CUDA events around the kernel on its
-          stream, L2 flushed (256 MB write) between steps.
+          inputs resident in HBM, CUDA events around the call on its stream,
+          L2 flushed (256 MB write) between steps.
   learned_warm_start : the same with the learned warm start, timed beside it.
   e2e   : the default path through the public host-array C entry point
-          assist_gb300_integrate_batch (H2D + kernel + D2H in the timed region).
-  roofline : FP64 pipe; achieved = algorithmic FP64 flops (oracle op count per
-          force evaluation x evaluations + IAS15 bookkeeping) / kernel time;
+          assist_gb300_integrate_batch (H2D + grouping + kernel + D2H in the
+          timed region), averaged over --steps calls.
+  roofline : FP64 pipe.  achieved = the FP64 work the kernel does / kernel
+          time: per force evaluation the particle-dependent force terms, per
+          body table (all bodies at one time, one per group and node time)
+          the ephemeris and the particle-independent force-term parts, plus
+          IAS15 bookkeeping (op counts from the oracle's counting type);
           peak = FP64 FMA throughput measured in this run.
   cpu_baseline : the oracle (CPU restatement of ASSIST's forces + IAS15) on all
-          host cores over a bounded random sample of the same population.
+          host cores over the population (bounded by a time budget).
+  parity : the GPU end states (plain and learned paths) against the oracle's
+          for every particle the CPU baseline integrated.
+  configs : the batched mixed-length population (65,536 particles, lengths
+          logU[30 d, 10 yr]) and the variational population (1,048,576
+          particles x 6 variational particles, lengths logU[30 d, 5 yr], 1% on
+          close Earth approaches), each timed with an oracle parity sample.
 
---impl reference times that CPU path alone (the reference arm).
-Multi-GPU (torchrun): weak scaling, each rank integrates its own batch of the
-same size; no collective on the data path.
+--impl reference times that CPU path alone (the reference arm); it loads no
+part of this library.  Multi-GPU (torchrun): weak scaling, each rank
+integrates its own batch of the same size; no collective on the data path.
 """
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import os
 import subprocess
@@ -56,50 +67,76 @@ WORKLOAD = "262144-mixture-1yr-learned-warm-start-vs-plain"
 METRIC = "particle-days/s FP64 on 1 GB300: learned-warm-start vs plain IAS15 vs CPU ref"
 UNIT = "particle-days/s"
 
+# IAS15 bookkeeping per force evaluation (predictor of x and v, divided
+# differences and b update) and per accepted step (compensated x, v update,
+# next-step prediction), FP64 operations per particle
+IAS_PER_EVAL = 3 * (34 + 16)
+IAS_PER_STEP = 3 * (2 * 9 + 2 * 8 + 8 + 7 * 8)
+
+# From one ncu capture of the block-cooperative kernel (three-blocks-per-SM
+# build) on the 32,768-particle case of this workload
+# (profiles/ag_k_coop_32768_mixture_1yr.md): DRAM bytes read + written per
+# particle-day of a launch, scaled to a full launch by its particle-days.
+DRAM_BYTES_PER_PARTICLE_DAY = 0.351
+
+
+def _synth():
+    """assist_gb300/synth.py loaded by path: it needs only numpy, and the
+    reference arm must not load the library (importing the package does)."""
+    name = "assist_gb300_synth_standalone"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, "assist_gb300", "synth.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
 
 def make_inputs(tmpdir: str):
-    from assist_gb300 import synth
+    synth = _synth()
     pl, ast, system = synth.write_ephemeris(tmpdir, seed=SEED_EPHEM, t_beg=T0 - 40.0, t_end=T0 + 3700.0)
     pop = synth.population(system, "mix", N_PARTICLES, seed=SEED_POP, t0=T0, length=LENGTH, nongrav_frac=0.1)
     return pl, ast, system, pop
 
 
-def algorithmic_flops(pl, ast, pop, stats):
-    """FP64 operations the outputs need: oracle op count of one force
-    evaluation (ephemeris of all bodies at the particle's own time + every
-    force term; sqrt and div counted as 1) times the evaluations, plus the
-    IAS15 predictor/corrector bookkeeping per evaluation and per step."""
+def op_model(pl, ast, pop):
+    """FP64 operations of one force evaluation from the oracle's counting
+    type (add, sub, mul = 1; div and sqrt = 1 each; no FMA credit), split into
+    the part that depends on the particle and the part a shared body table
+    does once: all bodies at one time plus the particle-independent pieces of
+    the force terms (origin-minus-body offsets, EIH source-source sums).
+    For a particle without non-gravitational parameters (90 % of the mix)."""
     from tests.oracle_py import Oracle
     o = Oracle(pl, ast)
     i_plain = int(np.nonzero(np.abs(pop.params).sum(1) == 0)[0][0])
     c = o.count_ops(T0, pop.state[i_plain])
-    per_eval = c["add"] + c["mul"] + c["div"] + c["sqrt"] + c["pow"]
-    ias_per_eval = 3 * (34 + 16)          # predictor x,v (9 + 8 terms) and divided-difference/b update
-    ias_per_step = 3 * (2 * 9 + 2 * 8 + 8 + 7 * 8)   # accept update, compensated sums, next-step prediction
-    flops = stats["force_evals"] * (per_eval + ias_per_eval) + stats["steps_accepted"] * ias_per_step
-    return flops, per_eval, c
+    s = lambda d: int(sum(d[k] for k in ("add", "mul", "div", "sqrt", "pow")))
+    bodies, shared, total = s(c["bodies"]), s(c["shared"]), s(c)
+    return {"per_eval_particle": total - bodies, "per_body_table": bodies + shared,
+            "per_eval_independent": total + shared, "ias15_per_eval": IAS_PER_EVAL, "ias15_per_step": IAS_PER_STEP,
+            "op_counts": {k: c[k] for k in ("add", "mul", "div", "sqrt", "pow")},
+            "op_counts_bodies": c["bodies"], "op_counts_shared": c["shared"]}
 
 
-def train_warm_start(eph, system, dev, n_train: int = N_TRAIN, steps: int = 1500):
-    """Log (features, target) pairs from one plain integration of a separate
-    seeded population of the same mixture (lengths logU[30 d, 10 yr]) and
-    train the warm-start network with the device kernels (outside the timed
-    region)."""
-    import torch
-    from assist_gb300 import synth, warm
-    tp = synth.population(system, "mix", n_train, seed=SEED_POP + 1, t0=T0, log_len=(30.0, 3652.5), nongrav_frac=0.1)
-    t = time.perf_counter()
-    warm.init(SEED_POP)
-    X, T, _ = warm.collect(eph, torch.tensor(tp.t0, device=dev), torch.tensor(tp.t_end, device=dev),
-                           torch.tensor(tp.state, device=dev), params=torch.tensor(tp.params, device=dev),
-                           capacity=5 << 20, every=1)
-    perm = torch.randperm(X.shape[0], device=dev, generator=torch.Generator(device=dev).manual_seed(0))
-    X, T = X[perm].contiguous(), T[perm].clamp(-4, 4).contiguous()
-    l0, _ = warm.grad(X[:4096], T[:4096])
-    loss = warm.train(X, T, steps=steps, batch=4096, lr=1e-3, seed=1)
-    torch.cuda.synchronize()
-    return {"pairs": int(X.shape[0]), "train_particles": n_train, "train_steps": steps, "batch": 4096,
-            "loss_initial": l0, "loss_final": loss, "train_s": time.perf_counter() - t}
+def roofline(stats, model, kernel_s, peak, pdays):
+    """FP64 roofline of the IAS15 kernel from its counters."""
+    ev, tabs, acc = stats["force_evals"], stats["tables_built"], stats["steps_accepted"]
+    work = ev * (model["per_eval_particle"] + IAS_PER_EVAL) + tabs * model["per_body_table"] + acc * IAS_PER_STEP
+    indep = ev * (model["per_eval_independent"] + IAS_PER_EVAL) + acc * IAS_PER_STEP
+    roof = {"bound": "fp64", "achieved": work / kernel_s / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": work / kernel_s / peak, "traffic": DRAM_BYTES_PER_PARTICLE_DAY * pdays,
+            "traffic_unit": "DRAM bytes per launch (ncu, 32,768-particle case of this kernel, scaled by particle-days)",
+            "peak_source": "measured in this run (FP64 FMA chains; MEASURED_PEAKS.json has no FP64 figure)",
+            "work": "per force evaluation %d flop of particle-dependent force terms + %d IAS15; per body table "
+                    "%d flop (ephemeris + particle-independent force-term parts); per accepted step %d"
+                    % (model["per_eval_particle"], IAS_PER_EVAL, model["per_body_table"], IAS_PER_STEP),
+            "flops_per_launch": work, "force_evals": ev, "body_tables": tabs,
+            "frac_vs_independent": indep / kernel_s / peak,
+            "frac_vs_independent_note": "the work of independent steps (every evaluation evaluating all bodies at "
+                                        "its own time, %d flop + IAS15) per the kernel's evaluations: a throughput "
+                                        "ratio against that algorithm, not pipe occupancy" % model["per_eval_independent"],
+            "model": model}
+    return roof
 
 
 class ClockSampler:
@@ -108,7 +145,6 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.rows = []
-        self._stop = threading.Event()
         self._p = None
 
     def start(self):
@@ -146,30 +182,45 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def cpu_baseline(pl, ast, pop, target_s: float = 15.0, threads=None):
-    """Oracle batch integration on the host cores over a random sample."""
-    from tests.oracle_py import Oracle
-    o = Oracle(pl, ast)
-    threads = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(7)
-    n_pilot = 4 * threads
-    idx = rng.choice(pop.t0.size, size=n_pilot, replace=False)
+def oracle_batch(o, pop, idx, threads, var=None, chunk=16384, budget_s=None):
+    """The oracle's independent integrations of particles idx (in chunks, all
+    threads), stopping after the chunk that passes budget_s.  Returns the
+    indices done, their end states, statuses (and variational states) and
+    the wall time."""
+    done, states, stats, vstates = [], [], [], []
     t = time.perf_counter()
-    o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx], threads=threads)
-    pilot = time.perf_counter() - t
-    n = int(min(pop.t0.size, max(n_pilot, n_pilot * target_s / max(pilot, 1e-3))))
-    idx = rng.choice(pop.t0.size, size=n, replace=False)
-    t = time.perf_counter()
-    _, _, st, _ = o.integrate_batch(pop.t0[idx], pop.t_end[idx], pop.state[idx], params=pop.params[idx],
-                                    threads=threads, return_all=True)
-    dt = time.perf_counter() - t
-    pdays = float(np.abs(pop.t_end[idx] - pop.t0[idx])[st == 0].sum())
-    return {"value": pdays / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d of the %d particles (random, seed 7), their full integrations: %.3g particle-days in %.1f s"
-                      % (n, pop.t0.size, pdays, dt)}
+    for k in range(0, len(idx), chunk):
+        j = idx[k:k + chunk]
+        st, vs, s, _ = o.integrate_batch(pop.t0[j], pop.t_end[j], pop.state[j], params=pop.params[j],
+                                         var_state=None if var is None else var[j], threads=threads, return_all=True)
+        done.append(j); states.append(st); stats.append(s)
+        if var is not None:
+            vstates.append(vs)
+        if budget_s is not None and time.perf_counter() - t > budget_s:
+            break
+    wall = time.perf_counter() - t
+    return (np.concatenate(done), np.concatenate(states), np.concatenate(stats),
+            np.concatenate(vstates) if vstates else None, wall)
+
+
+def parity(idx, ref, rstat, gpu, gstat, vref=None, vgpu=None):
+    """End-state agreement on the particles idx (both completed)."""
+    both = (rstat == 0) & (gstat[idx] == 0)
+    d = np.abs(gpu[idx][both, :3] - ref[both, :3]).max(axis=1) if both.any() else np.zeros(1)
+    out = {"n": int(both.sum()), "sampled": int(len(idx)), "median_au": float(np.median(d)), "max_au": float(d.max()),
+           "over_1e-9": int((d > 1e-9).sum()), "status_mismatches": int((rstat != gstat[idx]).sum())}
+    if vref is not None:
+        vg = vgpu[idx][both]
+        vr = vref[both]
+        rel = np.abs(vg - vr).max(axis=(1, 2)) / np.maximum(np.abs(vr).max(axis=(1, 2)), 1e-300)
+        out["variational_rel_max"] = float(rel.max()) if rel.size else 0.0
+        out["variational_rel_median"] = float(np.median(rel)) if rel.size else 0.0
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the oracle's IAS15 over the workload on all host
+    threads, nothing of this library loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -209,6 +260,89 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def timed_batch(batch, eph, t0, te, st0, prm, o, steps, warmup, stream, flush, world=1, var0=None, dist=None):
+    """W untimed then K timed passes of integrate_batch_device over the same
+    inputs (state reset before each); CUDA events around each call on its
+    stream.  Returns (ms total, summed stats, status, end state, var end
+    state, wall seconds)."""
+    import torch
+    dev = st0.device
+    st = st0.clone()
+    var = None if var0 is None else var0.clone()
+    status = torch.zeros(st0.shape[0], dtype=torch.int32, device=dev)
+    for _ in range(warmup):
+        st.copy_(st0)
+        if var is not None:
+            var.copy_(var0)
+        batch.integrate_batch_device(eph, t0, te, st, params=prm, var_state=var, status=status, opts=o, stream=stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs, acc = [], None
+    wall0 = time.perf_counter()
+    for _ in range(steps):
+        flush.fill_(1.0)
+        st.copy_(st0)
+        if var is not None:
+            var.copy_(var0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s = batch.integrate_batch_device(eph, t0, te, st, params=prm, var_state=var, status=status, opts=o,
+                                         stream=stream)
+        e1.record(stream)
+        evs.append((e0, e1))
+        if acc is None:
+            acc = dict(s)
+        else:
+            for k in s:
+                acc[k] += s[k]
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    wall = time.perf_counter() - wall0
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, acc, status.cpu().numpy(), st.cpu().numpy(), None if var is None else var.cpu().numpy(), wall
+
+
+def ias15_summary(acc, steps):
+    return {"kernel_ms_per_step": acc["kernel_ms"] / steps,
+            "steps_accepted": acc["steps_accepted"] // steps, "steps_rejected": acc["steps_rejected"] // steps,
+            "force_evals": acc["force_evals"] // steps, "body_tables": acc["tables_built"] // steps,
+            "iterations_per_step": acc["pc_iterations"] / max(acc["steps_accepted"] + acc["steps_rejected"], 1)}
+
+
+def extra_config(name, desc, batch, eph, o_cpu, pop, opts, steps, warmup, stream, flush, dev, sample, threads,
+                 var=None):
+    """One more configuration of the batched path: timed passes and an oracle
+    parity sample."""
+    import torch
+    t0 = torch.tensor(pop.t0, device=dev)
+    te = torch.tensor(pop.t_end, device=dev)
+    st0 = torch.tensor(pop.state, device=dev)
+    prm = torch.tensor(pop.params, device=dev)
+    v0 = None if var is None else torch.tensor(var, device=dev)
+    ms, acc, stat, st, vst, _ = timed_batch(batch, eph, t0, te, st0, prm, opts, steps, warmup, stream, flush, var0=v0)
+    done = stat == 0
+    pdays = float(np.abs(pop.t_end - pop.t0)[done].sum())
+    rng = np.random.default_rng(5)
+    idx = np.sort(rng.choice(pop.t0.size, size=min(sample, pop.t0.size), replace=False))
+    didx, ref, rstat, vref, cpu_s = oracle_batch(o_cpu, pop, idx, threads, var=var, chunk=max(len(idx), 1))
+    status_counts = {str(k): int(v) for k, v in zip(*np.unique(stat, return_counts=True))}
+    del t0, te, st0, prm, v0
+    return {"name": name, "description": desc, "n_particles": int(pop.t0.size),
+            "n_var_per_particle": 0 if var is None else 6, "value": pdays * steps / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup, "particle_days_per_step": pdays,
+            "ias15": ias15_summary(acc, steps), "status_counts": status_counts,
+            "parity": parity(didx, ref, rstat, st, stat, vref, vst),
+            "parity_oracle_s": cpu_s}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -217,9 +351,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="plain predictor only (no learned warm start)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the extra configuration lines")
     ap.add_argument("--blocks-per-sm", type=int, default=0,
                     help="block-cooperative kernel residency: 0 automatic (the library's choice), 2 or 3")
     ap.add_argument("--particles", type=int, default=None, help="override the batch size (profiling only)")
+    ap.add_argument("--cpu-budget-s", type=float, default=60.0,
+                    help="time budget of the oracle's CPU baseline / parity pass over the population")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -235,9 +372,10 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from assist_gb300 import Ephem, batch
+    from assist_gb300 import Ephem, batch, warm
     tmp = tempfile.mkdtemp(prefix="assist_bench_")
     pl, ast, system, pop = make_inputs(tmp)
+    synth = _synth()
     eph = Ephem(pl, ast)
     dev = torch.device("cuda", local)
     t0 = torch.tensor(pop.t0, device=dev)
@@ -250,49 +388,29 @@ def main():
     warm_opts = batch.options(group_steps=2, warm_start=1)
     warm_info = None
     if not args.no_warm:
-        warm_info = train_warm_start(eph, system, dev)
-
-    def timed(o):
-        st = st0.clone()
-        status = torch.zeros(N_PARTICLES, dtype=torch.int32, device=dev)
-        for _ in range(args.warmup):
-            st.copy_(st0)
-            batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=o, stream=stream)
+        # pairs logged from a plain run of a separate population, training by
+        # the device kernels (outside every timed region)
+        tp = synth.population(system, "mix", N_TRAIN, seed=SEED_POP + 1, t0=T0, log_len=(30.0, 3652.5),
+                              nongrav_frac=0.1)
+        t = time.perf_counter()
+        warm.init(SEED_POP)
+        X, T, _ = warm.collect(eph, torch.tensor(tp.t0, device=dev), torch.tensor(tp.t_end, device=dev),
+                               torch.tensor(tp.state, device=dev), params=torch.tensor(tp.params, device=dev),
+                               capacity=5 << 20, every=1)
+        perm = torch.randperm(X.shape[0], device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+        X, T = X[perm].contiguous(), T[perm].clamp(-4, 4).contiguous()
+        l0, _ = warm.grad(X[:4096], T[:4096])
+        loss = warm.train(X, T, steps=1500, batch=4096, lr=1e-3, seed=1)
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
-        evs, acc = [], None
-        wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            st.copy_(st0)
-            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            s = batch.integrate_batch_device(eph, t0, te, st, params=prm, status=status, opts=o, stream=stream)
-            e1.record(stream)
-            evs.append((e0, e1))
-            if acc is None:
-                acc = dict(s)
-            else:
-                for k in ("steps_accepted", "steps_rejected", "force_evals", "pc_iterations", "kernel_ms",
-                          "warm_start_used", "warm_start_fallback"):
-                    acc[k] += s[k]
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        wall = time.perf_counter() - wall0
-        ms = sum(a.elapsed_time(b) for a, b in evs)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, acc, status.cpu().numpy(), st, wall
+        warm_info = {"pairs": int(X.shape[0]), "train_particles": N_TRAIN, "train_steps": 1500, "batch": 4096,
+                     "loss_initial": l0, "loss_final": loss, "train_s": time.perf_counter() - t}
+        del X, T
 
     # the learned warm start, measured beside the plain predictor (the default path)
-    learned = None
+    learned, lstat, lst = None, None, None
     if not args.no_warm:
-        lms, lacc, lstat, lst, _ = timed(warm_opts)
+        lms, lacc, lstat, lst, _, _ = timed_batch(batch, eph, t0, te, st0, prm, warm_opts, args.steps, args.warmup,
+                                                  stream, flush, world, dist=dist)
         ldone = lstat == 0
         learned = {"value": world * float(np.abs(pop.t_end - pop.t0)[ldone].sum()) * args.steps / (lms / 1e3),
                    "unit": UNIT, "ms_per_step": lms / args.steps,
@@ -301,51 +419,84 @@ def main():
                    "used": lacc["warm_start_used"] // args.steps, "fallback": lacc["warm_start_fallback"] // args.steps}
     clocks = ClockSampler(local)
     clocks.start()
-    ms, stats_acc, st_host, st_dev, wall = timed(opts)
+    ms, stats_acc, st_host, st_end, _, wall = timed_batch(batch, eph, t0, te, st0, prm, opts, args.steps, args.warmup,
+                                                           stream, flush, world, dist=dist)
     clocks.stop()
     # particle-days of the particles that reached t_end (a particle that hits a
     # body stops with status 4 and its span is not counted)
     done = st_host == 0
     pdays = float(np.abs(pop.t_end - pop.t0)[done].sum())
-    bad = int((~done).sum())
     status_counts = {str(k): int(v) for k, v in zip(*np.unique(st_host, return_counts=True))}
     value = world * pdays * args.steps / (ms / 1e3)
     if learned is not None:
-        both = done & ldone
-        d = np.abs(st_dev.cpu().numpy()[both, :3] - lst.cpu().numpy()[both, :3]).max(axis=1)
-        learned["ratio_to_plain"] = learned["value"] / (world * pdays * args.steps / (ms / 1e3))
+        both = done & (lstat == 0)
+        d = np.abs(st_end[both, :3] - lst[both, :3]).max(axis=1)
+        learned["ratio_to_plain"] = learned["value"] / value
         learned["end_state_vs_plain_au"] = {"median": float(np.median(d)), "max": float(d.max()),
                                             "particles_over_1e-9": int((d > 1e-9).sum()),
                                             "status_mismatches": int((st_host != lstat).sum())}
         learned.update(warm_info)
-    # e2e through the host-array C entry point
+    # e2e through the host-array C entry point (inputs from host memory, end
+    # states and statuses back to it every call), averaged over --steps calls
     e2e = None
     if rank == 0:
         h_st = pop.state.copy()
-        t = time.perf_counter()
-        out, _, hstat, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, h_st, params=pop.params, opts=opts)
-        e2e_s = time.perf_counter() - t
+        batch.integrate_batch(eph, pop.t0, pop.t_end, h_st, params=pop.params, opts=opts)     # untimed
+        e2e_s, e2e_days = 0.0, 0.0
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            out, _, hstat, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, h_st, params=pop.params, opts=opts)
+            e2e_s += time.perf_counter() - t
+            e2e_days += float(np.abs(pop.t_end - pop.t0)[hstat == 0].sum())
         h2d = pop.t0.nbytes * 2 + pop.state.nbytes + pop.params.nbytes
         d2h = pop.state.nbytes + hstat.nbytes
-        e2e = {"value": float(np.abs(pop.t_end - pop.t0)[hstat == 0].sum()) / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        e2e = {"value": e2e_days / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "calls": args.steps, "ms_per_call": 1e3 * e2e_s / args.steps}
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
-    flops, per_eval, counts = algorithmic_flops(pl, ast, pop, stats_acc)
+    model = op_model(pl, ast, pop)
     kernel_s = stats_acc["kernel_ms"] / 1e3
     peak = batch.fp64_peak_gflops() * 1e9
-    achieved = flops / kernel_s
-    # DRAM bytes per launch: 0.351 B per particle-day, from one ncu capture of
-    # this kernel (three-blocks-per-SM build) on the 32,768-particle case of
-    # this workload (dram__bytes_read + dram__bytes_write: 4.20 MB for 11.97M
-    # particle-days), scaled by the particle-days of a full launch
-    traffic = 0.351 * pdays
-    roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (scaled from ncu)",
-            "peak_source": "measured in this run (FP64 FMA chains; MEASURED_PEAKS.json has no FP64 figure)",
-            "flops_per_force_eval": per_eval, "op_counts_per_eval": counts}
-    cpu = None if args.no_cpu_baseline else cpu_baseline(pl, ast, pop)
+    roof = roofline(stats_acc, model, kernel_s, peak, pdays)
+    # CPU baseline and parity: the oracle over the population (random order,
+    # all host threads, bounded by --cpu-budget-s), its end states compared
+    # with the GPU's
+    from tests.oracle_py import Oracle
+    o_cpu = Oracle(pl, ast)
+    threads = os.cpu_count() or 1
+    cpu, par, par_learned = None, None, None
+    if not args.no_cpu_baseline:
+        order = np.random.default_rng(7).permutation(pop.t0.size)
+        didx, ref, rstat, _, cpu_s = oracle_batch(o_cpu, pop, order, threads, budget_s=args.cpu_budget_s)
+        cdays = float(np.abs(pop.t_end[didx] - pop.t0[didx])[rstat == 0].sum())
+        cpu = {"value": cdays / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d of the %d particles (random order, seed 7), their full integrations: %.4g particle-days "
+                         "in %.1f s" % (len(didx), pop.t0.size, cdays, cpu_s)}
+        par = parity(didx, ref, rstat, st_end, st_host)
+        if learned is not None:
+            par_learned = parity(didx, ref, rstat, lst, lstat)
+            learned["parity_vs_oracle"] = par_learned
+    configs = None
+    if not args.no_configs and world == 1:
+        configs = []
+        p2 = synth.population(system, "mix", 65536, seed=SEED_POP + 2, t0=T0, log_len=(30.0, 3652.5),
+                              nongrav_frac=0.1)
+        configs.append(extra_config(
+            "batched-65536-mixture-10yr", "65,536 independent particles of the 40/30/20/10 mixture, lengths "
+            "logU[30 d, 10 yr], 10% non-gravitational, block-cooperative groups", batch, eph, o_cpu, p2,
+            batch.options(group_steps=2), 3, 3, stream, flush, dev, 2048, threads))
+        del p2
+        p4 = synth.population(system, "mix", 1 << 20, seed=SEED_POP + 4, t0=T0, log_len=(30.0, 1826.25),
+                              nongrav_frac=0.1, close_frac=0.01)
+        v4 = np.tile(np.eye(6)[None], (p4.t0.size, 1, 1))
+        configs.append(extra_config(
+            "variational-1048576x6-mixture-5yr", "1,048,576 particles of the mixture, each with 6 first-order "
+            "variational particles (unit deviations), lengths logU[30 d, 5 yr], 10% non-gravitational, 1% on close "
+            "Earth approaches (q_min logU[1e-4, 1e-2] AU); plain predictor; value counts real particle-days",
+            batch, eph, o_cpu, p4, batch.options(group_steps=2), 1, 1, stream, flush, dev, 512, threads, var=v4))
+        del p4, v4
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .440/SPK ephemeris, seeded population)",
@@ -357,16 +508,11 @@ def main():
                        "parallelism": "dp%d (independent batches, no collective)" % world},
             # per step: the encounter pilot's two kernels and the IAS15 kernel
             "gpu_launches": 3 * args.steps,
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "parity": par,
             "clocks": clocks.summary(),
-            "ias15": {"kernel_ms_per_step": stats_acc["kernel_ms"] / args.steps,
-                      "steps_accepted": stats_acc["steps_accepted"] // args.steps,
-                      "steps_rejected": stats_acc["steps_rejected"] // args.steps,
-                      "force_evals": stats_acc["force_evals"] // args.steps,
-                      "iterations_per_step": stats_acc["pc_iterations"] / max(stats_acc["steps_accepted"] +
-                                                                              stats_acc["steps_rejected"], 1)},
-            "unfinished_particles": bad, "status_counts": status_counts, "wall_s_timed_region": wall,
-            "learned_warm_start": learned}
+            "ias15": ias15_summary(stats_acc, args.steps),
+            "unfinished_particles": int((~done).sum()), "status_counts": status_counts,
+            "wall_s_timed_region": wall, "learned_warm_start": learned, "configs": configs}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

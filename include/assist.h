@@ -242,6 +242,9 @@ struct assist_gb300_batch_stats {
     long long warm_start_used;      /* steps whose learned start was accepted */
     long long warm_start_fallback;  /* steps that fell back to the plain predictor */
     double kernel_ms;               /* device time of the integration kernels */
+    long long tables_built;         /* body tables evaluated (all bodies at one time): one per
+                                       evaluation with independent steps, one per group and
+                                       node time with shared steps */
 };
 
 /* Integrate n independent test particles, each from t0[i] to t_end[i] (days

@@ -43,6 +43,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "dd.h"
@@ -58,6 +59,8 @@ enum { F_SUN = 0x01, F_PLANETS = 0x02, F_AST = 0x04, F_NONGRAV = 0x08, F_EARTH_H
 /* ---------------------------------------------------------------- counting */
 struct OpTally { long long add, mul, div, sqrt, fn; };
 static thread_local OpTally g_tally;
+static thread_local OpTally g_tally_bodies;
+static thread_local OpTally g_tally_shared;
 struct cnt {
     double v;
     cnt() : v(0) {}
@@ -78,11 +81,32 @@ static inline bool operator==(cnt a, cnt b) { return a.v == b.v; }
 static inline bool operator!=(cnt a, cnt b) { return a.v != b.v; }
 static inline cnt sqrt(cnt a) { g_tally.sqrt++; return cnt(std::sqrt(a.v)); }
 static inline cnt pow(cnt a, double y) { g_tally.fn++; return cnt(std::pow(a.v, y)); }
+
+/* Counting aid: move the operations tallied since `before` to the shared
+ * tally, the work of a force evaluation that does not depend on the particle
+ * (a kernel that shares one body table among many particles does it once per
+ * table). */
+static inline void tally_to_shared(const OpTally& before) {
+    g_tally_shared.add += g_tally.add - before.add; g_tally_shared.mul += g_tally.mul - before.mul;
+    g_tally_shared.div += g_tally.div - before.div; g_tally_shared.sqrt += g_tally.sqrt - before.sqrt;
+    g_tally_shared.fn += g_tally.fn - before.fn;
+    g_tally.add = before.add; g_tally.mul = before.mul; g_tally.div = before.div; g_tally.sqrt = before.sqrt;
+    g_tally.fn = before.fn;
+}
 static inline cnt floor(cnt a) { return cnt(std::floor(a.v)); }
 static inline double to_double(cnt a) { return a.v; }
 
 using std::sqrt;
 static inline double pow(double a, double y) { return std::pow(a, y); }
+
+/* The origin-minus-body half (xo - x_body) of a particle-body separation:
+ * the same subtraction, tallied when counting as particle-independent work. */
+template <class T>
+static inline T osub(const T& a, const T& b) {
+    T r = a - b;
+    if constexpr (std::is_same<T, cnt>::value) { g_tally.add--; g_tally_shared.add++; }
+    return r;
+}
 static inline double floor(double a) { return std::floor(a); }
 
 /* ---------------------------------------------------------------- files */
@@ -355,6 +379,21 @@ static Ephem* ephem_load(const char* planets, const char* asteroids) {
 
 /* ---------------------------------------------------------------- bodies */
 
+/* Sub-interval and normalised time of tt = record fraction x niv, as
+ * src/ascii_ephem.c:35-39 forms them: tau = 2 fmod(tt, 1) - 1 (fmod(tt, 1) is
+ * tt - trunc(tt), exactly) and b = (int)tt.  A time a rounding below a record
+ * boundary can give a tiny negative tt: b = 0 and tau just below -1, the start
+ * of the record.  At tt == niv exactly the reference reads one sub-interval
+ * past the column; here b stays in the last sub-interval, at its end
+ * (tau = +1). */
+template <class T>
+static T subinterval_tau(T tt, int niv, int* b) {
+    *b = (int)to_double(tt);
+    T ip = T(std::trunc(to_double(tt)));
+    if (*b >= niv) { *b = niv - 1; ip = T((double)(niv - 1)); }
+    return 2.0 * (tt - ip) - 1.0;
+}
+
 /* Chebyshev series for one column over its sub-interval: position (T),
  * velocity (S = dT/dtau, times c) and acceleration (U = d2T/dtau2, times c^2),
  * src/ascii_ephem.c:27-65. */
@@ -362,10 +401,9 @@ template <class T>
 static void cheb_column(const double* P, int ncm, int ncf, int niv, T tfrac, double inc, T* u, T* v, T* w) {
     T Tp[32], Sp[32], Up[32];
     T tt = tfrac * (double)niv;
-    T fl = floor(tt);
-    T tau = 2.0 * (tt - fl) - 1.0;
+    int blk;
+    T tau = subinterval_tau(tt, niv, &blk);
     double c = (double)(niv * 2) / inc / 86400.0;
-    int blk = (int)to_double(tt);
     Tp[0] = 1.0; Tp[1] = tau;
     Sp[0] = 0.0; Sp[1] = 1.0;
     Up[0] = 0.0; Up[1] = 0.0; Up[2] = 4.0;
@@ -428,9 +466,8 @@ static void cheb_column_need(const double* P, int ncm, int ncf, int niv, T tfrac
     if (vel) { cheb_column(P, ncm, ncf, niv, tfrac, inc, u, v, w); return; }
     T Tp[32];
     T tt = tfrac * (double)niv;
-    T fl = floor(tt);
-    T tau = 2.0 * (tt - fl) - 1.0;
-    int blk = (int)to_double(tt);
+    int blk;
+    T tau = subinterval_tau(tt, niv, &blk);
     Tp[0] = 1.0; Tp[1] = tau;
     for (int p = 2; p < ncf; p++) Tp[p] = 2.0 * tau * Tp[p - 1] - Tp[p - 2];
     for (int m = 0; m < ncm; m++) {
@@ -644,6 +681,7 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         out[1] = p[0] + B[1]; out[2] = p[1] + B[2]; out[3] = p[2] + B[3];
         for (int k = 4; k < 10; k++) out[k] = NAN;
     }
+    if constexpr (std::is_same<T, cnt>::value) g_tally_bodies = g_tally;   /* the body-state part of the count */
     auto GM = [&](int i) { return B[(size_t)i * 10]; };
     auto BX = [&](int i, int k) { return B[(size_t)i * 10 + 1 + k]; };
     auto BV = [&](int i, int k) { return B[(size_t)i * 10 + 4 + k]; };
@@ -664,16 +702,16 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         for (int j = 0; j < n_real; j++) {
             double A1 = params[3 * j], A2 = params[3 * j + 1], A3 = params[3 * j + 2];
             if (A1 == 0. && A2 == 0. && A3 == 0.) continue;
-            T dx = x[3 * j] + (xo[0] - BX(B_SUN, 0));
-            T dy = x[3 * j + 1] + (xo[1] - BX(B_SUN, 1));
-            T dz = x[3 * j + 2] + (xo[2] - BX(B_SUN, 2));
+            T dx = x[3 * j] + osub(xo[0], BX(B_SUN, 0));
+            T dy = x[3 * j + 1] + osub(xo[1], BX(B_SUN, 1));
+            T dz = x[3 * j + 2] + osub(xo[2], BX(B_SUN, 2));
             T r2 = dx * dx + dy * dy + dz * dz;
             T r = sqrt(r2);
             T rr0 = r / o.r0;
             T g = o.alpha * pow(rr0, -o.nm) * pow(1.0 + pow(rr0, o.nn), -o.nk);
-            T dvx = v[3 * j] + (vo[0] - BV(B_SUN, 0));
-            T dvy = v[3 * j + 1] + (vo[1] - BV(B_SUN, 1));
-            T dvz = v[3 * j + 2] + (vo[2] - BV(B_SUN, 2));
+            T dvx = v[3 * j] + osub(vo[0], BV(B_SUN, 0));
+            T dvy = v[3 * j + 1] + osub(vo[1], BV(B_SUN, 1));
+            T dvz = v[3 * j + 2] + osub(vo[2], BV(B_SUN, 2));
             T hx = dy * dvz - dz * dvy, hy = dz * dvx - dx * dvz, hz = dx * dvy - dy * dvx;
             T h = sqrt(hx * hx + hy * hy + hz * hz);
             T tx = hy * dz - hz * dy, ty = hz * dx - hx * dz, tz = hx * dy - hy * dx;
@@ -750,9 +788,9 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         const double ra = 0.0 * M_PI / 180., dec = 90.0 * M_PI / 180.;
         const double ca = std::cos(ra), sa = std::sin(ra), cd = std::cos(dec), sd = std::sin(dec);
         for (int j = 0; j < n_real; j++) {
-            T dx = x[3 * j] + (xo[0] - BX(B_EAR, 0));
-            T dy = x[3 * j + 1] + (xo[1] - BX(B_EAR, 1));
-            T dz = x[3 * j + 2] + (xo[2] - BX(B_EAR, 2));
+            T dx = x[3 * j] + osub(xo[0], BX(B_EAR, 0));
+            T dy = x[3 * j + 1] + osub(xo[1], BX(B_EAR, 1));
+            T dz = x[3 * j + 2] + osub(xo[2], BX(B_EAR, 2));
             T r2 = dx * dx + dy * dy + dz * dz;
             T r = sqrt(r2);
             T px = -dx * sa + dy * ca;
@@ -829,9 +867,9 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         const double ra = 286.13 * M_PI / 180., dec = 63.87 * M_PI / 180.;
         const double ca = std::cos(ra), sa = std::sin(ra), cd = std::cos(dec), sd = std::sin(dec);
         for (int j = 0; j < n_real; j++) {
-            T dx = x[3 * j] + (xo[0] - BX(B_SUN, 0));
-            T dy = x[3 * j + 1] + (xo[1] - BX(B_SUN, 1));
-            T dz = x[3 * j + 2] + (xo[2] - BX(B_SUN, 2));
+            T dx = x[3 * j] + osub(xo[0], BX(B_SUN, 0));
+            T dy = x[3 * j + 1] + osub(xo[1], BX(B_SUN, 1));
+            T dz = x[3 * j + 2] + osub(xo[2], BX(B_SUN, 2));
             T r2 = dx * dx + dy * dy + dz * dz;
             T r = sqrt(r2);
             T px = -dx * sa + dy * ca;
@@ -878,7 +916,7 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
             for (int a = 0; a < 3; a++) { for (int b = 0; b < 6; b++) { J[a][b] = 0.0; dt7[a][b] = 0.0; } for (int b = 0; b < 3; b++) dt8[a][b] = 0.0; }
             T vi[3] = {v[3 * i], v[3 * i + 1], v[3 * i + 2]};
             for (int jj = 0; jj < o.gr_eih_sources; jj++) {
-                T dij[3] = {x[3 * i] + (xo[0] - BX(jj, 0)), x[3 * i + 1] + (xo[1] - BX(jj, 1)), x[3 * i + 2] + (xo[2] - BX(jj, 2))};
+                T dij[3] = {x[3 * i] + osub(xo[0], BX(jj, 0)), x[3 * i + 1] + osub(xo[1], BX(jj, 1)), x[3 * i + 2] + osub(xo[2], BX(jj, 2))};
                 T rij2 = dij[0] * dij[0] + dij[1] * dij[1] + dij[2] * dij[2];
                 T rij = sqrt(rij2);
                 T pre = GM(jj) / (rij2 * rij);
@@ -900,18 +938,22 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
                 T aj[3] = {0.0, 0.0, 0.0};
                 T dterm0[3] = {0.0, 0.0, 0.0};
                 for (int k = 0; k < NPL; k++) {
-                    T dik[3] = {x[3 * i] + (xo[0] - BX(k, 0)), x[3 * i + 1] + (xo[1] - BX(k, 1)), x[3 * i + 2] + (xo[2] - BX(k, 2))};
+                    T dik[3] = {x[3 * i] + osub(xo[0], BX(k, 0)), x[3 * i + 1] + osub(xo[1], BX(k, 1)), x[3 * i + 2] + osub(xo[2], BX(k, 2))};
                     T rik2 = dik[0] * dik[0] + dik[1] * dik[1] + dik[2] * dik[2];
                     T rik = sqrt(rik2);
                     term0 += GM(k) / rik;
                     if (want_var) for (int a = 0; a < 3; a++) dterm0[a] -= GM(k) / (rik * rik * rik) * dik[a];
                     if (k != jj) {
+                        /* source-source sums: the same for every particle */
+                        OpTally before{};
+                        if constexpr (std::is_same<T, cnt>::value) before = g_tally;
                         T djk[3] = {BX(jj, 0) - BX(k, 0), BX(jj, 1) - BX(k, 1), BX(jj, 2) - BX(k, 2)};
                         T rjk2 = djk[0] * djk[0] + djk[1] * djk[1] + djk[2] * djk[2];
                         T rjk = sqrt(rjk2);
                         term1 += GM(k) / rjk;
                         T fac = GM(k) / (rjk2 * rjk);
                         for (int a = 0; a < 3; a++) aj[a] -= fac * djk[a];
+                        if constexpr (std::is_same<T, cnt>::value) tally_to_shared(before);
                     }
                 }
                 term0 *= -2 * (beta + gamma) * oc2;
@@ -973,7 +1015,7 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         const double C2 = e.c_squared;
         const T GMs = GM(B_SUN);
         for (int j = 0; j < n_real; j++) {
-            T p[3] = {x[3 * j] + (xo[0] - BX(B_SUN, 0)), x[3 * j + 1] + (xo[1] - BX(B_SUN, 1)), x[3 * j + 2] + (xo[2] - BX(B_SUN, 2))};
+            T p[3] = {x[3 * j] + osub(xo[0], BX(B_SUN, 0)), x[3 * j + 1] + osub(xo[1], BX(B_SUN, 1)), x[3 * j + 2] + osub(xo[2], BX(B_SUN, 2))};
             T r2 = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
             T r = sqrt(r2);
             T pre = -6.0 * GMs * GMs / (C2 * r2 * r2);
@@ -998,8 +1040,8 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
         for (int j = 0; j < n_real; j++) {
             T p[3], pv[3];
             for (int a = 0; a < 3; a++) {
-                p[a] = x[3 * j + a] + (xo[a] - BX(B_SUN, a));
-                pv[a] = v[3 * j + a] + (vo[a] - BV(B_SUN, a));
+                p[a] = x[3 * j + a] + osub(xo[a], BX(B_SUN, a));
+                pv[a] = v[3 * j + a] + osub(vo[a], BV(B_SUN, a));
             }
             T v2 = pv[0] * pv[0] + pv[1] * pv[1] + pv[2] * pv[2];
             T r = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
@@ -1036,9 +1078,9 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
             if (b > B_SUN && b < NPL && !(o.forces & F_PLANETS)) continue;
             if (b >= NPL && !(o.forces & F_AST)) continue;
             for (int j = 0; j < n_real; j++) {
-                T dx = x[3 * j] + (xo[0] - BX(b, 0));
-                T dy = x[3 * j + 1] + (xo[1] - BX(b, 1));
-                T dz = x[3 * j + 2] + (xo[2] - BX(b, 2));
+                T dx = x[3 * j] + osub(xo[0], BX(b, 0));
+                T dy = x[3 * j + 1] + osub(xo[1], BX(b, 1));
+                T dz = x[3 * j + 2] + osub(xo[2], BX(b, 2));
                 T r2 = dx * dx + dy * dy + dz * dz;
                 T r = sqrt(r2);
                 T pre = GM(b) / (r * r * r);
@@ -1055,9 +1097,9 @@ static int forces(const Ephem& e, const ForceOpts& o, T t, int n_real, const T* 
             int b = k >= na ? order[k - na] : k + NPL;
             for (int j = 0; j < n_real; j++) {
                 if (vars[(size_t)j].empty()) continue;
-                T dx = x[3 * j] + (xo[0] - BX(b, 0));
-                T dy = x[3 * j + 1] + (xo[1] - BX(b, 1));
-                T dz = x[3 * j + 2] + (xo[2] - BX(b, 2));
+                T dx = x[3 * j] + osub(xo[0], BX(b, 0));
+                T dy = x[3 * j + 1] + osub(xo[1], BX(b, 1));
+                T dz = x[3 * j + 2] + osub(xo[2], BX(b, 2));
                 T r2 = dx * dx + dy * dy + dz * dz;
                 T r = sqrt(r2);
                 T r3i = 1. / (r2 * r);
@@ -1205,7 +1247,7 @@ struct Ias15 {
     }
     /* One attempted step of size `h` (sign = direction).  Returns 1 accepted,
      * 0 rejected, <0 force error. */
-    int step(ForceFn<T>& F, T hstep, const IasOpts& o, IasStats& st, T* dt_new_out) {
+    int step(ForceFn<T>& F, T hstep, const IasOpts& o, IasStats& st, T* dt_new_out, bool cut = false) {
         const IasConst& C = K();
         const size_t n3 = 3 * (size_t)N, nr3 = 3 * (size_t)n_real;
         const double sgn = to_double(hstep) >= 0 ? 1.0 : -1.0;
@@ -1286,8 +1328,10 @@ struct Ias15 {
             if (std::isnormal(to_double(err))) dt_new = T(std::pow(o.epsilon / to_double(err), 1.0 / 7.0)) * dt_done;
             else dt_new = dt_done / safety;
             if (to_double(fabs(dt_new)) < o.min_dt) dt_new = T(std::copysign(o.min_dt, to_double(dt_new)));
-            /* step underflow (an impact): stop, keeping the state of the step start */
-            if (o.dt_floor > 0.0 && to_double(fabs(dt_new)) < o.dt_floor) { *dt_new_out = dt_new; return 2; }
+            /* step underflow (an impact): stop, keeping the state of the step start.
+             * Not on a step cut short to land on t_end: the proposal scales
+             * with that short step and says nothing about the orbit. */
+            if (!cut && o.dt_floor > 0.0 && to_double(fabs(dt_new)) < o.dt_floor) { *dt_new_out = dt_new; return 2; }
             T ratio = dt_new / dt_done;
             if (fabs(ratio) < T(safety)) {
                 // rejected: re-predict from the last accepted step, or start from zero
@@ -1338,7 +1382,7 @@ struct Ias15 {
             T h = dt;
             if (to_double(fabs(dt)) >= to_double(fabs(rem))) { h = rem; last = true; }
             T dtn;
-            int r = step(F, h, o, st, &dtn);
+            int r = step(F, h, o, st, &dtn, last);
             if (r < 0) { st.status = 1; return -r; }
             if (r == 2) { st.status = 4; return 0; }
             dt = dtn;
@@ -1433,7 +1477,10 @@ int orc_forces_dd(void* h, int fbits, int gr_eih_sources, int geocentric, const 
 
 /* Operation counts of one force evaluation for a single real particle (with
  * its n_var variational particles), including the evaluation of every body
- * at that particle's time.  out: add, mul, div, sqrt, pow. */
+ * at that particle's time.  out[0..4]: add, mul, div, sqrt, pow of the
+ * particle-dependent work and the body states; out[5..9]: the body-state part
+ * of out[0..4]; out[10..14]: force-term work that does not depend on the
+ * particle, tallied apart. */
 int orc_count_ops(void* h, int fbits, int gr_eih_sources, int geocentric, const double* law, double t,
                   const double* x, const double* v, int n_var, const double* vx, const double* vv,
                   const double* params, long long* out) {
@@ -1442,8 +1489,17 @@ int orc_count_ops(void* h, int fbits, int gr_eih_sources, int geocentric, const 
     std::vector<cnt> A(3 * (size_t)(1 + n_var));
     std::vector<int> vtp((size_t)n_var, 0);
     g_tally = OpTally{0, 0, 0, 0, 0};
+    g_tally_bodies = OpTally{0, 0, 0, 0, 0};
+    g_tally_shared = OpTally{0, 0, 0, 0, 0};
     int r = forces<cnt>(*(Ephem*)h, o, cnt(t), 1, X.data(), V.data(), n_var, vtp.data(), VX.data(), VV.data(), params, A.data());
     out[0] = g_tally.add; out[1] = g_tally.mul; out[2] = g_tally.div; out[3] = g_tally.sqrt; out[4] = g_tally.fn;
+    /* out[5..9]: the part of it that forms the body states (all bodies at t) */
+    out[5] = g_tally_bodies.add; out[6] = g_tally_bodies.mul; out[7] = g_tally_bodies.div;
+    out[8] = g_tally_bodies.sqrt; out[9] = g_tally_bodies.fn;
+    /* out[10..14]: force-term work that does not depend on the particle
+     * (origin-minus-body offsets, EIH source-source sums), not in out[0..4] */
+    out[10] = g_tally_shared.add; out[11] = g_tally_shared.mul; out[12] = g_tally_shared.div;
+    out[13] = g_tally_shared.sqrt; out[14] = g_tally_shared.fn;
     return r;
 }
 

@@ -102,6 +102,20 @@ def reference_outputs(R, e, system):
             bodies[k, i] = o
     g["body_times"] = times
     g["bodies"] = bodies
+    # body states at record and sub-interval edges: times a rounding below a
+    # 32-day record boundary (the Julian date rounds up across it, so the
+    # record fraction comes out a hair below zero), the boundaries themselves,
+    # and sub-interval boundaries inside a record
+    edges = np.array([8000.0 - 1e-10, 8032.0 - 2e-10, 8096.0 - 5e-11, 8160.0 - 2.2e-10, 8000.0, 8128.0,
+                      8008.0 - 1e-10, 8040.0, 8128.0 + 1e-10, 8004.0 - 3e-11])
+    eb = np.zeros((len(edges), 27, 10))
+    for k, t in enumerate(edges):
+        for i in range(27):
+            o = np.zeros(10)
+            assert R.refh_get_body(e, i, t, p(o)) == 0
+            eb[k, i] = o
+    g["edge_times"] = edges
+    g["edge_bodies"] = eb
     # force cases
     rng = np.random.default_rng(77)
     mba = synth.population(system, "mba", 12, seed=11, t0=8100.0)

@@ -125,13 +125,19 @@ class Oracle:
         prm = None
         if params is not None:
             prm = np.concatenate([np.asarray(params, np.float64).reshape(3), np.zeros(3 * m)])
-        out = np.zeros(5, dtype=np.int64)
+        out = np.zeros(15, dtype=np.int64)
         law = np.asarray(law, np.float64)
         r = self.lib.orc_count_ops(self.h, forces, gr_eih_sources, 0, _p(law), float(t), _p(x), _p(v), m, _p(vx),
                                    _p(vv), _p(prm), out.ctypes.data_as(L))
         if r != 0:
             raise RuntimeError("oracle count status %d" % r)
-        return dict(zip(["add", "mul", "div", "sqrt", "pow"], out.tolist()))
+        names = ["add", "mul", "div", "sqrt", "pow"]
+        d = dict(zip(names, out[:5].tolist()))
+        d["bodies"] = dict(zip(names, out[5:10].tolist()))    # the part of d that forms the body states
+        # force-term work that does not depend on the particle (origin-minus-body
+        # offsets, EIH source-source sums); counted apart from d
+        d["shared"] = dict(zip(names, out[10:15].tolist()))
+        return d
 
     def integrate(self, t0, t_end, state, var_state=None, var_tp=None, params=None, epsilon=1e-9, min_dt=0.0,
                   dt0=0.001, max_steps=0, dd=False, forces=0x7F, gr_eih_sources=1, geocentric=0, law=DEFAULT_LAW,

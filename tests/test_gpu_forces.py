@@ -106,6 +106,24 @@ def test_bodies_vs_oracle(synth_files, dev):
             assert np.abs(B[k, i, m] - ref[m]).max() <= 4e-16 * max(scale, 1.0), (t, i)
 
 
+def test_edge_bodies_vs_reference_golden(golden, golden_paths, dev):
+    """Bodies at record and sub-interval edges (a time a rounding below a
+    record boundary: the record fraction is a hair below zero, where the
+    reference's fmod keeps the record's start) against the reference."""
+    import torch
+    from assist_gb300 import batch
+    eph = _eph(golden_paths)
+    ts = golden["edge_times"]
+    B = batch.bodies_device(eph, torch.tensor(ts, device=dev)).cpu().numpy()
+    for k, t in enumerate(ts):
+        for i in range(27):
+            ref = golden["edge_bodies"][k, i]
+            m = np.isfinite(ref)
+            assert np.array_equal(np.isfinite(B[k, i]), m)
+            scale = np.abs(ref[m]).max()
+            assert np.abs(B[k, i, m] - ref[m]).max() <= 4e-16 * max(scale, 1.0), (t, i, B[k, i] - ref)
+
+
 def test_get_particle_and_coverage(golden, golden_paths, dev):
     eph = _eph(golden_paths)
     p = eph.get_particle("Sun", float(golden["body_times"][3]))

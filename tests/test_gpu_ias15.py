@@ -42,6 +42,24 @@ def test_batch_vs_oracle_mixture(synth_files, group_steps):
         assert np.median(dx) < 1e-11
 
 
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
+def test_batch_fixed_step_from_record_edge(golden_paths, group_steps):
+    """Fixed steps from a start time a rounding below a 32-day record
+    boundary (the body tables of the step start sit at a record fraction a
+    hair below zero) reproduce the oracle's, in every batched kernel."""
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    eph = _eph(golden_paths); O = Oracle(*golden_paths)
+    system = synth.SolarSystem(4242)
+    t0 = 8000.0 - 1e-10
+    pop = synth.population(system, "mix", 64, seed=21, t0=t0, length=2.0)
+    o = batch.options(group_steps=group_steps, epsilon=0.0, dt0=0.25)
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, opts=o)
+    ref, _, rstat, _ = O.integrate_batch(pop.t0, pop.t_end, pop.state, epsilon=0.0, dt0=0.25, return_all=True)
+    assert (status == 0).all() and (rstat == 0).all()
+    assert np.abs(out[:, :3] - ref[:, :3]).max() < 1e-13
+
+
 def test_batch_variational_vs_oracle(synth_files):
     from assist_gb300 import batch, synth
     from tests.oracle_py import Oracle
@@ -216,3 +234,26 @@ def test_batch_spk_planets_vs_oracle(synth_files_spk, group_steps):
     assert dx.max() < 1e-9, dx.max()
     if group_steps == 0:
         assert np.median(dx) < 1e-12
+
+
+@pytest.mark.parametrize("group_steps", [0, 1, 2])
+def test_batch_watchdog_marks_every_unfinished_particle(synth_files, monkeypatch, group_steps):
+    """With a run-time budget far below what the batch needs, the kernel
+    stops early: every particle it did not finish (taken or still queued)
+    says ASSIST_GB300_TIMEOUT (5); a particle reported complete (0) holds
+    its end state."""
+    from assist_gb300 import batch, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "mix", 4096, seed=41, t0=8000.0, log_len=(1.0, 400.0))
+    monkeypatch.setenv("ASSIST_GB300_WATCHDOG_S", "2e-4")
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state,
+                                              opts=batch.options(group_steps=group_steps))
+    monkeypatch.delenv("ASSIST_GB300_WATCHDOG_S")
+    assert set(np.unique(status)) <= {0, 5}, np.unique(status)
+    assert (status == 5).sum() > 2048
+    ok = np.nonzero(status == 0)[0]
+    if ok.size:
+        ref = O.integrate_batch(pop.t0[ok], pop.t_end[ok], pop.state[ok])
+        assert np.abs(out[ok, :3] - ref[:, :3]).max() < 1e-9

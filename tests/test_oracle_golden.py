@@ -19,6 +19,33 @@ def test_bodies_bitwise(golden, oracle_golden):
             assert np.array_equal(out[m], ref[m]), (t, i, out - ref)
 
 
+def test_edge_bodies_bitwise(golden, oracle_golden):
+    """Record and sub-interval edges: a time a rounding below a record
+    boundary (its Julian date rounds up across it, the record fraction comes
+    out a hair below zero), the boundaries, sub-interval boundaries."""
+    for k, t in enumerate(golden["edge_times"]):
+        for i in range(27):
+            st, out = oracle_golden.body(i, t)
+            assert st == 0
+            ref = golden["edge_bodies"][k, i]
+            m = ~np.isnan(ref)
+            assert np.array_equal(np.isnan(out), np.isnan(ref))
+            assert np.array_equal(out[m], ref[m]), (t, i, out - ref)
+
+
+def test_edge_bodies_continuous(golden, oracle_golden):
+    """Just below a record boundary the bodies are where they are at the
+    boundary (to their motion over the gap), not a sub-interval away."""
+    for t in golden["edge_times"]:
+        if t == round(t) or abs(t - round(t)) > 1e-9:
+            continue
+        tb = float(round(t))
+        for i in range(27):
+            _, a = oracle_golden.body(i, t)
+            _, b = oracle_golden.body(i, tb)
+            assert np.abs(a[1:4] - b[1:4]).max() < 1e-11, (t, i, a[1:4] - b[1:4])
+
+
 def test_forces_bitwise(golden, oracle_golden):
     st = golden["force_state"]
     n = st.shape[0]

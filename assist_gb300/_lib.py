@@ -45,7 +45,8 @@ class Options(ctypes.Structure):
                 ("alpha", c_double), ("nk", c_double), ("nm", c_double), ("nn", c_double), ("r0", c_double),
                 ("epsilon", c_double), ("min_dt", c_double), ("dt0", c_double), ("max_steps", c_int),
                 ("warm_start", c_int), ("threads_per_block", c_int), ("group_steps", c_int),
-                ("dt_floor", c_double), ("group_order", c_int), ("blocks_per_sm", c_int)]
+                ("dt_floor", c_double), ("group_order", c_int), ("blocks_per_sm", c_int),
+                ("ephem_staging", c_int)]
 
 
 class BatchStats(ctypes.Structure):
@@ -55,6 +56,24 @@ class BatchStats(ctypes.Structure):
                 ("kernel_ms", c_double), ("tables_built", c_longlong)]
 
 
+class TuneResult(ctypes.Structure):
+    """struct assist_gb300_tune_result (include/assist.h)."""
+    _fields_ = [("chosen", c_int), ("n_candidates", c_int), ("candidate", c_int * 4), ("kernel_ms", c_double * 4),
+                ("signature", ctypes.c_char * 512)]
+
+
+clib.assist_gb300_autotune_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p,
+                                              c_void_p, c_int, c_void_p, c_void_p, POINTER(TuneResult)]
+clib.assist_gb300_autotune_device.restype = c_int
+clib.assist_gb300_plan_create.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_int, c_void_p, c_void_p, c_void_p, POINTER(c_void_p)]
+clib.assist_gb300_plan_create.restype = c_int
+clib.assist_gb300_plan_launch.argtypes = [c_void_p, c_void_p]
+clib.assist_gb300_plan_launch.restype = c_int
+clib.assist_gb300_plan_stats.argtypes = [c_void_p, POINTER(BatchStats)]
+clib.assist_gb300_plan_stats.restype = c_int
+clib.assist_gb300_plan_free.argtypes = [c_void_p]
+clib.assist_gb300_plan_free.restype = None
 clib.assist_gb300_default_options.argtypes = [POINTER(Options)]
 clib.assist_gb300_default_options.restype = None
 clib.assist_gb300_integrate_batch.argtypes = [c_void_p, POINTER(Options), c_int, D, D, D, D, c_int, D, I,

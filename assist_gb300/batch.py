@@ -12,7 +12,7 @@ from typing import Optional
 
 import numpy as np
 
-from ._lib import BatchStats, D, I, Options, clib, last_error
+from ._lib import BatchStats, D, I, Options, TuneResult, clib, last_error
 from .ephem import Ephem
 
 
@@ -20,7 +20,7 @@ def options(**kw) -> Options:
     """ASSIST's defaults (src/assist.c:408-447) overridden by keyword arguments:
     forces, gr_eih_sources, geocentric, alpha, nk, nm, nn, r0, epsilon, min_dt,
     dt0, max_steps, warm_start, threads_per_block, group_steps, dt_floor,
-    group_order, blocks_per_sm (struct assist_gb300_options in assist.h)."""
+    group_order, blocks_per_sm, ephem_staging (struct assist_gb300_options in assist.h)."""
     o = Options()
     clib.assist_gb300_default_options(byref(o))
     for k, v in kw.items():
@@ -76,6 +76,67 @@ def integrate_batch_device(ephem: Ephem, t0, t_end, state, params=None, var_stat
     if rc != 0:
         raise RuntimeError("assist_gb300_integrate_batch_device failed (%d): %s" % (rc, last_error()))
     return {f: getattr(stats, f) for f, _ in BatchStats._fields_}
+
+
+def autotune_device(ephem: Ephem, t0, t_end, state, params=None, var_state=None, opts: Optional[Options] = None,
+                    stream=None) -> dict:
+    """Time the default batched kernel's builds on this batch (torch CUDA
+    tensors; the states are copied, not changed) and record the fastest for
+    batches of its signature (assist_gb300_autotune_device).  Returns the
+    chosen build (2, 3: plain, blocks per SM; 4: plain, two with the staged
+    .440 record; 5: the learned warm start, a candidate when opts.warm_start
+    is set), each candidate's kernel time and the signature."""
+    o = opts or options()
+    r = TuneResult()
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_autotune_device(byref(ephem), byref(o), state.shape[0], _ptr(t0), _ptr(t_end), _ptr(state),
+                                           _ptr(params), 0 if var_state is None else 6, _ptr(var_state), s, byref(r))
+    if rc != 0:
+        raise RuntimeError("assist_gb300_autotune_device failed (%d): %s" % (rc, last_error()))
+    names = {2: "2 blocks/SM", 3: "3 blocks/SM", 4: "2 blocks/SM + staged .440 record", 5: "learned warm start"}
+    return {"chosen": r.chosen, "chosen_name": names.get(r.chosen, "?"),
+            "candidates_ms": {names[r.candidate[k]]: r.kernel_ms[k] for k in range(r.n_candidates)},
+            "signature": r.signature.decode()}
+
+
+class Plan:
+    """A batch integrated repeatedly (assist_gb300_plan_*): the host work of a
+    call done once, each launch a CUDA-graph replay over the same device
+    tensors.  Write the next initial states into ``state`` (in place) between
+    launches."""
+
+    def __init__(self, ephem: Ephem, t0, t_end, state, params=None, var_state=None, status=None,
+                 opts: Optional[Options] = None, stream=None):
+        o = opts or options()
+        self._keep = (ephem, t0, t_end, state, params, var_state, status)
+        self._h = c_void_p()
+        s = None if stream is None else c_void_p(stream.cuda_stream)
+        rc = clib.assist_gb300_plan_create(byref(ephem), byref(o), state.shape[0], _ptr(t0), _ptr(t_end), _ptr(state),
+                                           _ptr(params), 0 if var_state is None else 6, _ptr(var_state), _ptr(status),
+                                           s, byref(self._h))
+        if rc != 0:
+            raise RuntimeError("assist_gb300_plan_create failed (%d): %s" % (rc, last_error()))
+
+    def launch(self, stream=None) -> None:
+        s = None if stream is None else c_void_p(stream.cuda_stream)
+        rc = clib.assist_gb300_plan_launch(self._h, s)
+        if rc != 0:
+            raise RuntimeError("assist_gb300_plan_launch failed (%d): %s" % (rc, last_error()))
+
+    def stats(self) -> dict:
+        st = BatchStats()
+        rc = clib.assist_gb300_plan_stats(self._h, byref(st))
+        if rc != 0:
+            raise RuntimeError("assist_gb300_plan_stats failed (%d): %s" % (rc, last_error()))
+        return {f: getattr(st, f) for f, _ in BatchStats._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            clib.assist_gb300_plan_free(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        self.close()
 
 
 def integrate_batch_dense_device(ephem: Ephem, t0, t_end, state, out_start, out_t, out_state, params=None,

@@ -19,7 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libassist_gb300.so")
-SOURCES = ["kernels_forces.cu", "kernels_ias15.cu", "kernels_shared.cu", "static_batch.cu", "kernels_mlp.cu", "kernels_pilot.cu", "host_ephem.cpp", "api.cpp"]
+SOURCES = ["kernels_forces.cu", "kernels_ias15.cu", "kernels_coop.cu", "kernels_shared.cu", "static_batch.cu", "kernels_mlp.cu",
+           "kernels_pilot.cu", "host_ephem.cpp", "api.cpp", "autotune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-lineinfo",
           "--expt-relaxed-constexpr", "-I", CSRC, "-I", os.path.join(ROOT, "include")]

@@ -543,6 +543,7 @@ extern "C" void assist_gb300_default_options(struct assist_gb300_options* o) {
     o->dt_floor = 1e-8;
     o->group_order = 0;
     o->blocks_per_sm = 0;
+    o->ephem_staging = 0;
 }
 
 extern "C" int assist_gb300_n_bodies(const struct assist_ephem* e) { return ag_ephem_n_bodies(e); }
@@ -859,28 +860,47 @@ static void ag_group_form(std::vector<AgGroupKey>& key, const float* ratio, int 
     gsize.swap(z2);
 }
 
-static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
-                              const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
-                              int n_var, double* d_var_state, int* d_status, void* stream,
-                              struct assist_gb300_batch_stats* stats, const int* d_out_start, const double* d_out_t,
-                              double* d_out_state) {
+/* Option checks of the batched entry points. */
+static int ag_batch_validate(const struct assist_gb300_options* o, int n_var) {
+    if (!o) { ag_set_error("options are required"); return ASSIST_ERROR_N; }
     if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
-    if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
     if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
-    if (o->warm_start && (o->group_steps != 2 || n_var != 0)) {
-        ag_set_error("the learned warm start runs in the block-cooperative kernel: group_steps = 2, n_var = 0");
+    if (o->warm_start < 0 || o->warm_start > 3 || (o->warm_start && o->group_steps != 2)) {
+        ag_set_error("warm_start is 0, 1, 2 or 3; the learned warm start runs in the block-cooperative kernel "
+                     "(group_steps = 2)");
+        return ASSIST_ERROR_N;
+    }
+    if (o->ephem_staging < 0 || o->ephem_staging > 2 || (o->ephem_staging == 1 && o->blocks_per_sm == 3)) {
+        ag_set_error("ephem_staging must be 0, 1 or 2; staging runs two blocks per SM (blocks_per_sm 0 or 2)");
         return ASSIST_ERROR_N;
     }
     if (o->warm_start && !ag_mlp_device_view()) {
         ag_set_error("warm_start = 1 needs a network (assist_gb300_warm_init, _set_params or _train first)");
         return ASSIST_ERROR_N;
     }
+    return ASSIST_SUCCESS;
+}
+
+/* What a batched launch needs from the host: the device view, the force
+ * model, the queue order and groups, and the kernel build.  The inputs are
+ * read back through g_batch's pinned staging and the encounter pilot runs
+ * in g_batch's buffers, so the caller holds g_batch_mu. */
+struct AgLaunchPlan {
+    DevEphem D;
+    ForceCfg c;
+    std::vector<int> order, gstart, gsize;
+    bool grouped = false, coop = false;
+    bool learned = false;           /* the warm-start build of the block-cooperative kernel */
+    int occ = 2, stage = 0, tpb = 128, nslots = 0;
+};
+
+static int ag_batch_prepare(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                            const double* d_t0, const double* d_t_end, const double* d_state, const double* d_params,
+                            int n_var, cudaStream_t s, AgLaunchPlan& P) {
     DevEphem D;
     int st = ag_ephem_device(e, &D);
     if (st) return st;
     const ForceCfg c = make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
-    cudaStream_t s = (cudaStream_t)stream;
-    std::lock_guard<std::mutex> lk(g_batch_mu);
     const bool grouped = o->group_steps != 0;
     /* block size (independent steps): 128 threads, halved (down to one warp)
      * while the batch would leave SMs idle */
@@ -975,16 +995,39 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         if (ag_cuda_check(cudaStreamSynchronize(s), "pilot kernels")) return ASSIST_ERROR_EPHEM_FILE;
         ag_group_form(key, enc, o->group_order, order, gstart, gsize);
     }
-    int nslots, occ = 2;
+    int nslots, occ = 2, stage = 0;
     const bool coop = o->group_steps == 2;
     if (coop) {
         /* one 32-particle group per 128-thread block */
         /* three resident blocks per SM (the plain kernel's 168-register
          * build) when the batch has at least 8 groups per such block: the
          * throughput gain outweighs the slower longest groups; two otherwise */
-        if (n_var == 0 && !o->warm_start) {
-            if (o->blocks_per_sm == 2 || o->blocks_per_sm == 3) {
+        float *lx = nullptr, *lt = nullptr;
+        int lcap = 0, levery = 1, *lcnt = nullptr;
+        const bool log_on = ag_mlp_log_config(&lx, &lt, &lcap, &levery, &lcnt) != 0;
+        const std::string key = ag_tune_key((int)gstart.size(), n, t0, te, has_ng.data(), c.forces, c.gr_eih_sources,
+                                            c.geocentric, e->spk_planets ? 1 : 0) +
+                                (n_var ? "|nv6" : "") + (o->warm_start ? "|warm" : "");
+        ag_tune_note(key);
+        int tuned = 0;
+        if (o->warm_start) {
+            /* the learned warm start unless the autotuner found the plain
+             * predictor faster on a batch of this signature (warm_start = 1;
+             * 2 runs the learned start regardless) */
+            tuned = o->warm_start == 1 ? ag_tune_lookup(key) : 0;   /* 2, 3: the learned start regardless */
+            P.learned = !(tuned >= 2 && tuned <= 4);
+        } else if (o->ephem_staging == 0 && o->blocks_per_sm == 0) {
+            tuned = ag_tune_lookup(key);
+        }
+        if (log_on) P.learned = true;      /* pairs are logged by the warm-start build */
+        if (n_var == 0 && !P.learned) {
+            if (o->ephem_staging == 1 || tuned == 4) {
+                occ = 2;
+                stage = e->spk_planets ? 0 : 1;
+            } else if (o->blocks_per_sm == 2 || o->blocks_per_sm == 3) {
                 occ = o->blocks_per_sm;
+            } else if (tuned == 2 || tuned == 3) {
+                occ = tuned;              /* recorded by assist_gb300_autotune_device for this signature */
             } else {
                 int dev = 0, sms = 0;
                 cudaGetDevice(&dev);
@@ -992,7 +1035,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
                 occ = (int)gstart.size() >= 8 * 3 * sms ? 3 : 2;
             }
         }
-        nslots = ag_coop_max_slots(n_var, occ);
+        nslots = ag_coop_max_slots(n_var, occ, stage, P.learned ? 1 : 0);
         const int need = 32 * (int)gstart.size();
         if (nslots > need) nslots = need;
     } else if (grouped) {
@@ -1003,6 +1046,39 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         nslots = ag_batch_max_slots(n_var, tpb);
         if (nslots > n) nslots = n;
     }
+    P.D = D;
+    P.c = c;
+    P.order.swap(order);
+    P.gstart.swap(gstart);
+    P.gsize.swap(gsize);
+    P.grouped = grouped;
+    P.coop = coop;
+    P.occ = occ;
+    P.stage = stage;
+    P.tpb = tpb;
+    P.nslots = nslots;
+    return ASSIST_SUCCESS;
+}
+
+static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                              const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
+                              int n_var, double* d_var_state, int* d_status, void* stream,
+                              struct assist_gb300_batch_stats* stats, const int* d_out_start, const double* d_out_t,
+                              double* d_out_state) {
+    int rc = ag_batch_validate(o, n_var);
+    if (rc) return rc;
+    if (n <= 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    AgLaunchPlan P;
+    if ((rc = ag_batch_prepare(e, o, n, d_t0, d_t_end, d_state, d_params, n_var, s, P))) return rc;
+    const DevEphem& D = P.D;
+    const ForceCfg& c = P.c;
+    const std::vector<int>& order = P.order;
+    const std::vector<int>& gstart = P.gstart;
+    const std::vector<int>& gsize = P.gsize;
+    const bool grouped = P.grouped, coop = P.coop;
+    const int occ = P.occ, stage = P.stage, tpb = P.tpb, nslots = P.nslots;
     if (g_batch.order_cap < n) {
         if (g_batch.d_order) cudaFree(g_batch.d_order);
         if (ag_cuda_check(cudaMalloc(&g_batch.d_order, sizeof(int) * (size_t)n), "cudaMalloc(order)")) return ASSIST_ERROR_EPHEM_FILE;
@@ -1045,8 +1121,9 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
     a.dt_floor = o->dt_floor;
     if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
     a.out_start = d_out_start; a.out_t = d_out_t; a.out_state = d_out_state;
-    if (coop && n_var == 0) {
+    if (coop && P.learned) {
         if (o->warm_start) a.mlp = ag_mlp_device_view();
+        a.warm_no_time_fallback = o->warm_start == 3 ? 1 : 0;
         float *lx = nullptr, *lt = nullptr;
         int cap = 0, every = 1, *cnt = nullptr;
         if (ag_mlp_log_config(&lx, &lt, &cap, &every, &cnt)) {
@@ -1060,7 +1137,7 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0); cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int le = coop ? ag_launch_coop(D, c, a, n_var, occ, s)
+    int le = coop ? ag_launch_coop(D, c, a, n_var, occ, stage, s)
                   : (grouped ? ag_launch_group(D, c, a, n_var, s) : ag_launch_batch(D, c, a, n_var, tpb, s));
     cudaEventRecord(e1, s);
     if (le) { cudaEventDestroy(e0); cudaEventDestroy(e1); ag_cuda_check((cudaError_t)le, "batch kernel launch"); return ASSIST_ERROR_EPHEM_FILE; }
@@ -1080,6 +1157,151 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         stats->kernel_ms = ms;
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return ASSIST_SUCCESS;
+}
+
+/* ---------------------------------------------------------------- plans
+ * A batch integrated again and again with the same particles' times and
+ * grouping (new initial states written into the same device arrays between
+ * launches: clones of an orbit, Monte Carlo samples, restarts): the host
+ * work of a call (read-back, encounter pilot, sort, upload) is done once, and
+ * each launch replays a CUDA graph of the device work (queue and counter
+ * reset, the persistent kernel, the counters' copy to pinned host memory). */
+struct assist_gb300_plan {
+    int n = 0;
+    int device = 0;
+    AgLaunchPlan P;
+    AgBatchArgs a;
+    int* d_order = nullptr;
+    int* d_grp = nullptr;
+    int* d_queue = nullptr;
+    unsigned long long* d_counters = nullptr;
+    double* d_ws = nullptr;
+    unsigned long long* h_counters = nullptr;     /* pinned, written by the graph */
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t last = nullptr;                  /* stream of the last launch */
+    long long launches = 0;
+};
+
+extern "C" void assist_gb300_plan_free(struct assist_gb300_plan* p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->d_order) cudaFree(p->d_order);
+    if (p->d_grp) cudaFree(p->d_grp);
+    if (p->d_queue) cudaFree(p->d_queue);
+    if (p->d_counters) cudaFree(p->d_counters);
+    if (p->d_ws) cudaFree(p->d_ws);
+    if (p->h_counters) cudaFreeHost(p->h_counters);
+    delete p;
+}
+
+extern "C" int assist_gb300_plan_create(const struct assist_ephem* e, const struct assist_gb300_options* o, int n,
+                                        const double* d_t0, const double* d_t_end, double* d_state,
+                                        const double* d_params, int n_var, double* d_var_state, int* d_status,
+                                        void* stream, struct assist_gb300_plan** out) {
+    if (!out) { ag_set_error("plan: an output pointer is required"); return ASSIST_ERROR_N; }
+    *out = nullptr;
+    int rc = ag_batch_validate(o, n_var);
+    if (rc) return rc;
+    if (n <= 0 || !d_t0 || !d_t_end || !d_state || (n_var && !d_var_state)) {
+        ag_set_error("plan: n > 0 and the batch's device arrays are required");
+        return ASSIST_ERROR_N;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    assist_gb300_plan* p = new assist_gb300_plan();
+    p->n = n;
+    cudaGetDevice(&p->device);
+    {
+        std::lock_guard<std::mutex> lk(g_batch_mu);
+        if ((rc = ag_batch_prepare(e, o, n, d_t0, d_t_end, d_state, d_params, n_var, s, p->P))) {
+            delete p;
+            return rc;
+        }
+    }
+    const AgLaunchPlan& P = p->P;
+    const int ng = (int)P.gstart.size();
+    const size_t wsn = ag_batch_ws_doubles(P.nslots, n_var);
+    bool ok = !ag_cuda_check(cudaMalloc(&p->d_order, sizeof(int) * (size_t)n), "cudaMalloc(plan order)") &&
+              (!P.grouped || !ag_cuda_check(cudaMalloc(&p->d_grp, sizeof(int) * 2 * (size_t)ng), "cudaMalloc(plan groups)")) &&
+              !ag_cuda_check(cudaMalloc(&p->d_queue, sizeof(int)), "cudaMalloc(plan queue)") &&
+              !ag_cuda_check(cudaMalloc(&p->d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc(plan counters)") &&
+              !ag_cuda_check(cudaMalloc(&p->d_ws, sizeof(double) * wsn), "cudaMalloc(plan IAS15 slots)") &&
+              !ag_cuda_check(cudaMallocHost(&p->h_counters, 8 * sizeof(unsigned long long)), "cudaMallocHost(plan counters)") &&
+              !ag_cuda_check(cudaMemcpy(p->d_order, P.order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "plan order") &&
+              (!P.grouped ||
+               (!ag_cuda_check(cudaMemcpy(p->d_grp, P.gstart.data(), sizeof(int) * (size_t)ng, cudaMemcpyHostToDevice), "plan groups") &&
+                !ag_cuda_check(cudaMemcpy(p->d_grp + ng, P.gsize.data(), sizeof(int) * (size_t)ng, cudaMemcpyHostToDevice), "plan groups"))) &&
+              !ag_cuda_check((cudaError_t)ag_batch_ready(), "batched kernel set-up") &&
+              !ag_cuda_check((cudaError_t)ag_coop_ready(), "batched kernel set-up");
+    if (!ok) { assist_gb300_plan_free(p); return ASSIST_ERROR_EPHEM_FILE; }
+    AgBatchArgs& a = p->a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = n; a.nslots = P.nslots; a.order = p->d_order; a.queue = p->d_queue;
+    a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
+    a.status = d_status; a.ws = p->d_ws; a.counters = p->d_counters;
+    a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
+    a.dt_floor = o->dt_floor;
+    if (P.grouped) { a.grp_start = p->d_grp; a.grp_size = p->d_grp + ng; a.n_groups = ng; }
+    if (P.coop && P.learned && o->warm_start) a.mlp = ag_mlp_device_view();
+    a.warm_no_time_fallback = o->warm_start == 3 ? 1 : 0;
+    double wd = 300.0;
+    if (const char* w = getenv("ASSIST_GB300_WATCHDOG_S")) wd = atof(w);
+    a.watchdog_cycles = wd > 0 ? (long long)(wd * 2.1e9) : 0;
+    /* capture the device work on a private stream */
+    cudaStream_t cs = nullptr;
+    if (ag_cuda_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "plan capture stream")) {
+        assist_gb300_plan_free(p);
+        return ASSIST_ERROR_EPHEM_FILE;
+    }
+    int le = 0;
+    ok = !ag_cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "plan capture");
+    if (ok) {
+        cudaMemsetAsync(p->d_queue, 0, sizeof(int), cs);
+        cudaMemsetAsync(p->d_counters, 0, 8 * sizeof(unsigned long long), cs);
+        le = P.coop ? ag_launch_coop(P.D, P.c, a, n_var, P.occ, P.stage, cs)
+                    : (P.grouped ? ag_launch_group(P.D, P.c, a, n_var, cs) : ag_launch_batch(P.D, P.c, a, n_var, P.tpb, cs));
+        cudaMemcpyAsync(p->h_counters, p->d_counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs);
+        const cudaError_t ce = cudaStreamEndCapture(cs, &p->graph);
+        ok = !le && !ag_cuda_check(ce, "plan capture") &&
+             !ag_cuda_check(cudaGraphInstantiate(&p->exec, p->graph, 0), "plan graph instantiate");
+    }
+    cudaStreamDestroy(cs);
+    if (!ok) {
+        if (le) ag_cuda_check((cudaError_t)le, "plan kernel capture");
+        assist_gb300_plan_free(p);
+        return ASSIST_ERROR_EPHEM_FILE;
+    }
+    *out = p;
+    return ASSIST_SUCCESS;
+}
+
+extern "C" int assist_gb300_plan_launch(struct assist_gb300_plan* p, void* stream) {
+    if (!p || !p->exec) { ag_set_error("plan: no plan"); return ASSIST_ERROR_N; }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != p->device) { ag_set_error("plan: launched on another device than it was made on"); return ASSIST_ERROR_N; }
+    if (ag_cuda_check(cudaGraphLaunch(p->exec, (cudaStream_t)stream), "plan graph launch")) return ASSIST_ERROR_EPHEM_FILE;
+    p->last = (cudaStream_t)stream;
+    p->launches++;
+    return ASSIST_SUCCESS;
+}
+
+extern "C" int assist_gb300_plan_stats(struct assist_gb300_plan* p, struct assist_gb300_batch_stats* stats) {
+    if (!p || !stats) { ag_set_error("plan: plan and stats are required"); return ASSIST_ERROR_N; }
+    std::memset(stats, 0, sizeof(*stats));
+    if (!p->launches) return ASSIST_SUCCESS;
+    if (ag_cuda_check(cudaStreamSynchronize(p->last), "plan launch")) return ASSIST_ERROR_EPHEM_FILE;
+    const unsigned long long* cnt = p->h_counters;
+    stats->steps_accepted = (long long)cnt[0];
+    stats->steps_rejected = (long long)cnt[1];
+    stats->force_evals = (long long)cnt[2];
+    stats->pc_iterations = (long long)cnt[3];
+    stats->warm_start_used = (long long)cnt[4];
+    stats->warm_start_fallback = (long long)cnt[5];
+    stats->tables_built = (long long)cnt[6];
+    stats->kernel_ms = -1.0;    /* not timed: time a launch with events on its stream */
     return ASSIST_SUCCESS;
 }
 

@@ -194,13 +194,22 @@ static ascii_s* ascii_load(const char* path) {
     a->find("GM8", &a->mass[ASSIST_BODY_NEPTUNE]); a->find("GM9", &a->mass[ASSIST_BODY_PLUTO]);
     a->find("J2E", &a->J2E); a->find("J3E", &a->J3E); a->find("J4E", &a->J4E); a->find("J2SUN", &a->J2SUN);
     a->find("AU", &a->AU); a->find("RE", &a->RE); a->find("CLIGHT", &a->CLIGHT); a->find("ASUN", &a->ASUN);
-    if (ag_cuda_check(cudaMalloc(&a->d_data, a->data.size() * 8), "cudaMalloc(.440 records)") ||
+    return a;
+}
+
+/* The device copy of the .440 image, made on first device use (loading and
+ * validating a file is host work only). */
+static int ascii_upload(ascii_s* a) {
+    if (a->d_data) return 0;
+    /* 64 bytes of padding: a record staged by a bulk copy is read from its
+     * address rounded down to 16 bytes, for its length rounded up */
+    if (ag_cuda_check(cudaMalloc(&a->d_data, a->data.size() * 8 + 64), "cudaMalloc(.440 records)") ||
         ag_cuda_check(cudaMemcpy(a->d_data, a->data.data(), a->data.size() * 8, cudaMemcpyHostToDevice), "upload .440")) {
         if (a->d_data) cudaFree(a->d_data);
-        delete a;
-        return nullptr;
+        a->d_data = nullptr;
+        return ASSIST_ERROR_EPHEM_FILE;
     }
-    return a;
+    return 0;
 }
 
 static void ascii_free(ascii_s* a) {
@@ -289,6 +298,13 @@ static spk_s* spk_load(const char* path) {
             s->segs.push_back(g);
         }
     }
+    return s;
+}
+
+/* The device copies of an SPK image, its segment table and record metadata,
+ * made on first device use. */
+static int spk_upload(spk_s* s) {
+    if (s->d_data) return 0;
     bool ok = !ag_cuda_check(cudaMalloc(&s->d_data, s->data.size() * 8), "cudaMalloc(SPK)") &&
               !ag_cuda_check(cudaMemcpy(s->d_data, s->data.data(), s->data.size() * 8, cudaMemcpyHostToDevice), "upload SPK") &&
               !ag_cuda_check(cudaMalloc(&s->d_segs, sizeof(AgSpkSeg) * (s->segs.size() + 1)), "cudaMalloc(SPK segments)") &&
@@ -299,10 +315,10 @@ static spk_s* spk_load(const char* path) {
         if (s->d_data) cudaFree(s->d_data);
         if (s->d_segs) cudaFree(s->d_segs);
         if (s->d_meta) cudaFree(s->d_meta);
-        delete s;
-        return nullptr;
+        s->d_data = nullptr; s->d_segs = nullptr; s->d_meta = nullptr;
+        return ASSIST_ERROR_EPHEM_FILE;
     }
-    return s;
+    return 0;
 }
 
 static void spk_free(spk_s* s) {
@@ -376,7 +392,7 @@ static void spk_join_masses(spk_s* s, const spk_constants& k) {
 
 /* ---------------------------------------------------------------- device view */
 static void ag_ascii_view(const ascii_s* a, DevEphem& D);
-static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out);
+static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out, bool may_upload = true);
 
 /* The planets part of the view for a planets SPK file. */
 static void spk_planets_view(const struct assist_ephem* e, DevEphem& D) {
@@ -401,6 +417,9 @@ static void spk_planets_view(const struct assist_ephem* e, DevEphem& D) {
 
 int ag_ephem_device(const struct assist_ephem* e, DevEphem* out) {
     if (!e || (!e->ascii_planets && !e->spk_planets)) return ASSIST_ERROR_EPHEM_FILE;
+    if ((e->spk_planets && spk_upload(e->spk_planets)) || (e->ascii_planets && ascii_upload(e->ascii_planets)) ||
+        (e->spk_asteroids && spk_upload(e->spk_asteroids)))
+        return ASSIST_ERROR_EPHEM_FILE;
     DevEphem D;
     std::memset(&D, 0, sizeof(D));
     D.jd_ref = e->jd_ref;
@@ -431,7 +450,7 @@ static void ag_ascii_view(const ascii_s* a, DevEphem& D) {
 }
 
 /* Asteroids and constants, then the device copy of the view. */
-static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out) {
+static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* out, bool may_upload) {
     const spk_s* s = e->spk_asteroids;
     D.n_ast = 0;
     if (s) {
@@ -453,6 +472,21 @@ static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* o
     /* the view is owned by the planets object (one view per ephemeris) */
     DevEphem** d_view = e->spk_planets ? &e->spk_planets->d_view : &e->ascii_planets->d_view;
     DevEphem* h_view = e->spk_planets ? &e->spk_planets->h_view : &e->ascii_planets->h_view;
+    if (!may_upload) {
+        /* the device view must exist and match the ephemeris as it is now */
+        if (!*d_view) {
+            ag_set_error("the ephemeris has no device view yet: make one ordinary device call with it first");
+            return ASSIST_ERROR_EPHEM_FILE;
+        }
+        D.self_dev = *d_view;
+        if (std::memcmp(h_view, &D, sizeof(D)) != 0) {
+            ag_set_error("the ephemeris changed (jd_ref or a constant) since its device view was made: make one "
+                         "ordinary device call with it first");
+            return ASSIST_ERROR_EPHEM_FILE;
+        }
+        *out = D;
+        return ASSIST_SUCCESS;
+    }
     if (!*d_view && ag_cuda_check(cudaMalloc(d_view, sizeof(DevEphem)), "cudaMalloc(ephemeris view)"))
         return ASSIST_ERROR_EPHEM_FILE;
     D.self_dev = *d_view;
@@ -464,6 +498,21 @@ static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* o
     }
     *out = D;
     return ASSIST_SUCCESS;
+}
+
+int ag_ephem_device_current(const struct assist_ephem* e, DevEphem* out) {
+    if (!e || (!e->ascii_planets && !e->spk_planets)) return ASSIST_ERROR_EPHEM_FILE;
+    if ((e->spk_planets && !e->spk_planets->d_data) || (e->ascii_planets && !e->ascii_planets->d_data) ||
+        (e->spk_asteroids && !e->spk_asteroids->d_data)) {
+        ag_set_error("the ephemeris has no device copy yet: make one ordinary device call with it first");
+        return ASSIST_ERROR_EPHEM_FILE;
+    }
+    DevEphem D;
+    std::memset(&D, 0, sizeof(D));
+    D.jd_ref = e->jd_ref;
+    if (e->spk_planets) spk_planets_view(e, D);
+    else ag_ascii_view(e->ascii_planets, D);
+    return ag_finish_view(e, D, out, false);
 }
 
 int ag_ephem_view_ready(const struct assist_ephem* e) {

@@ -1,6 +1,6 @@
 /*
  * ias15_coop.cuh -- block-cooperative grouped batched IAS15 (included by
- * kernels_ias15.cu, after the warp-grouped kernel whose helpers it uses).
+ * kernels_coop.cu).
  *
  * A group of up to 32 particles that share their step times (the same
  * grouping as the warp-grouped kernel) is integrated by one 128-thread block:
@@ -93,12 +93,106 @@ struct AgCoopTab {
     double rel[AG_NPL + AG_MAX_AST][3];
 };
 
+/* ---- The active .440 record staged in shared memory by a bulk (TMA) copy.
+ *
+ * One thread issues cp.async.bulk of the record (1,018 doubles, 8,144 bytes
+ * for DE440's layout) from the device image into the block's buffer, with an
+ * mbarrier counting the bytes; every thread waits on the barrier's phase.
+ * Records are 32 days long, so a block re-stages only when its group's time
+ * crosses into the next record: the eight node tables of a step and the
+ * steps and groups after it read their Chebyshev coefficients from shared
+ * memory.  The copy starts at the record's address rounded down to 16 bytes
+ * and covers the record rounded up to 16 bytes (the device image carries 64
+ * bytes of padding), as the bulk copy requires. */
+#define AG_STAGE_BYTES 8192
+#define AG_STAGE_MAX_REC ((AG_STAGE_BYTES - 16) / 8)     /* largest record (doubles) that fits with its offset */
+#define AG_STAGE_WAIT_LIMIT (1 << 22)                    /* try_wait polls before a copy counts as lost */
+
+struct AgRecStage {
+    double buf[AG_STAGE_BYTES / 8];
+    unsigned long long bar;        /* mbarrier: one arrival (the issuing thread) + the copied bytes */
+};
+
+/* Per-thread view of the staging state: the record held (identical in every
+ * thread of the block) and the barrier phase to wait for next. */
+struct AgStageCursor {
+    const double* src = nullptr;
+    unsigned phase = 0;
+};
+
+__device__ __forceinline__ void ag_mbar_init(unsigned long long* bar) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+/* Bounded wait for the barrier's phase `parity`; false when it did not
+ * complete within AG_STAGE_WAIT_LIMIT polls. */
+__device__ __forceinline__ bool ag_mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    for (int it = 0; it < AG_STAGE_WAIT_LIMIT; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+/* Record `rec` (global) in the block's buffer: a bulk copy when it is not
+ * the record already held.  Every thread of the block calls it with the same
+ * rec.  Returns the record's first coefficient in shared memory; sets
+ * *fail when the copy did not complete. */
+__device__ __forceinline__ const double* ag_stage_record(const DevEphem& E, const double* rec, AgRecStage& R, int tid,
+                                                         AgStageCursor& cur, int* fail) {
+    const unsigned long long a = reinterpret_cast<unsigned long long>(rec);
+    const unsigned long long al = a & ~15ull;
+    const unsigned delta = (unsigned)(a - al);
+    if (rec != cur.src) {
+        const unsigned bytes = (delta + 8u * (unsigned)E.pl_rec_len + 15u) & ~15u;
+        if (tid == 0) {
+            const unsigned b = (unsigned)__cvta_generic_to_shared(&R.bar);
+            const unsigned d = (unsigned)__cvta_generic_to_shared(R.buf);
+            /* the buffer's previous contents were read by generic loads before
+             * the caller's last barrier; order them before the async write */
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(d), "l"(al), "r"(bytes), "r"(b)
+                         : "memory");
+        }
+        if (!ag_mbar_wait(&R.bar, cur.phase)) {
+            *fail = 1;
+            cur.src = nullptr;
+        } else {
+            cur.src = rec;
+        }
+        cur.phase ^= 1u;
+    }
+    return reinterpret_cast<const double*>(reinterpret_cast<const char*>(R.buf) + delta);
+}
+
 /* Table pass 1: column and asteroid component sums.  Returns this thread's
- * coverage status (combined by the caller's barrier). */
+ * coverage status (combined by the caller's barrier).  STAGE: the .440
+ * coefficients come from the record staged in shared memory (R, cur); a lost
+ * copy sets *stage_fail. */
+template <bool STAGE>
 __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const ForceCfg& c, double t, AgCoopScratch& S,
-                                                   AgCoopTab& CT, int tid) {
+                                                   AgCoopTab& CT, int tid, AgRecStage* R, AgStageCursor& cur,
+                                                   int* stage_fail) {
     AgTable& T = CT.T;
     int bad = 0;
+    const double* srec = nullptr;    /* staged record (STAGE) */
+    double stf = 0.0;
+    if (STAGE && !E.pl_spk && E.pl_rec_len <= AG_STAGE_MAX_REC) {
+        const double* grec = nullptr;
+        if (ag_planet_record(E, t, &grec, &stf) == AG_OK) srec = ag_stage_record(E, grec, *R, tid, cur, stage_fail);
+    }
     if (E.pl_spk) {
         /* planets from an SPK file: one thread of warp 1 per body, full state
          * straight into the table (src/spk.c:550-608) */
@@ -115,9 +209,9 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
         const int lane = tid & 31;
         const bool w0 = tid < 32;
         if ((w0 && lane < 30) || (!w0 && lane < 3)) {
-            const double* rec = nullptr;
-            double tf = 0.0;
-            if (ag_planet_record(E, t, &rec, &tf) != AG_OK) {
+            const double* rec = srec;
+            double tf = stf;
+            if (!rec && ag_planet_record(E, t, &rec, &tf) != AG_OK) {
                 bad = 1;
             } else if (w0) {
                 /* MER..LUN (columns 0..9), component lane % 3 */
@@ -457,6 +551,8 @@ struct AgCoopShared {
     double rb6[3][32];                              /* |b6| of x, y, z after convergence */
     int fin[3][32];
     int g, stop;
+    int stage_fail;                                 /* a staged record copy did not complete */
+    int wg_off;                                     /* learned warm start switched off for this group */
 };
 
 /* Shared buffers of the learned warm start (dynamic shared memory, present
@@ -483,16 +579,20 @@ __device__ __forceinline__ double ag_nearest_planet(const AgTable& T, double x, 
 }
 
 /* Node-0 part of the learned warm start for one group (all threads of the
- * block call it): owners publish (br - er) and |b_pred|, warp 0 forms the
- * features, the block runs the network, owners add kappa_k y_kc to b.  Kept
- * out of line so the plain kernel's register allocation is not shaped by it. */
-__device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws, int nslots, int slot, AgWarmSmem& WS,
+ * block call it): owners publish (br - er) and |b_pred| of the particle's
+ * x, y, z (variational particles keep the plain prediction), warp 0 forms
+ * the features, the block runs the network, owners add kappa_k y_kc to b.
+ * Every 8th step of a group is a plain probe (no inference).  Returns whether
+ * the network ran (block-uniform).  Kept out of line so the plain kernel's
+ * register allocation is not shaped by it. */
+template <int NV>
+__device__ __noinline__ bool ag_coop_warm_start(const AgBatchArgs& A, double* ws, int nslots, int slot, AgWarmSmem& WS,
                                                const AgTable& Tab, int lane, int wid, bool live, bool warm, bool wl_on,
                                                double hstep, double dtls, long long steps, bool& w_applied,
                                                bool& w_probe, unsigned long long& n_wused,
                                                unsigned long long& n_wfall) {
-    const Ws<3> W{ws, nslots, slot};
-    const int pc = ag_coop_pcomp<0>(wid);
+    const Ws<3 * (1 + NV)> W{ws, nslots, slot};
+    const int pc = ag_coop_pcomp<NV>(wid);
     if (live && pc >= 0)
         for (int k = 0; k < 7; k++) {
             WS.corr[k][pc][lane] = W(W_BR + k, pc) - W(W_ER + k, pc);
@@ -520,7 +620,8 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
     const bool valid = live && WS.valid[lane];
     w_probe = warm && valid && wl_on && (steps & 7) == 7;
     const bool want = warm && valid && wl_on && !w_probe;
-    if (__syncthreads_or(want)) {
+    const bool ran = __syncthreads_or(want);
+    if (ran) {
         ag_mlp_infer_block(*A.mlp, WS.M, wid, lane);
         if (want) {
             bool ok_y = true;
@@ -539,6 +640,7 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
             }
         }
     }
+    return ran;
 }
 
 /* Dynamic shared memory of a block: the warm-start buffers (when present)
@@ -546,21 +648,25 @@ __device__ __noinline__ void ag_coop_warm_start(const AgBatchArgs& A, double* ws
  * state (40 fields x 3 components x 32 lanes, 30 KB).  Otherwise the state
  * stays in the global workspace, indexed by slot (both would not leave room
  * for two blocks per SM). */
-template <int NV, bool WARM>
+template <int NV, bool WARM, bool STAGE = false>
 struct AgCoopDyn {
     static constexpr bool ws_shared = NV == 0 && !WARM;
     static constexpr size_t warm = WARM ? (sizeof(AgWarmSmem) + 15) / 16 * 16 : 0;
     static constexpr size_t ws = ws_shared ? sizeof(double) * W_NF * 3 * 32 : 0;
-    static constexpr size_t bytes = warm + ws;
+    static constexpr size_t stage_off = warm + ws;        /* the staged .440 record (STAGE) */
+    static constexpr size_t stage = STAGE ? (sizeof(AgRecStage) + 15) / 16 * 16 : 0;
+    static constexpr size_t bytes = warm + ws + stage;
 };
 
 /* OCC: resident blocks per SM the kernel is compiled for.  The plain kernel
- * comes in two builds: 2 (236 registers) and 3 (168 registers, a few
- * spills: 1.5 % faster on batches with many groups per block, slower on
- * small batches whose longest groups set the time); the variational and
- * warm-start instantiations have only 2 (their Jacobians or network buffers
- * would spill or not fit). */
-template <int NV, bool WARM, int OCC = 2>
+ * comes in three builds: 2 (242 registers), 3 (168 registers, a few
+ * spills: faster on batches with many groups per block, slower on small
+ * batches whose longest groups set the time), and 2 with the active .440
+ * record staged in shared memory by bulk copies (STAGE; its 8 KB buffer does
+ * not fit beside three blocks); the variational and warm-start
+ * instantiations have only 2 (their Jacobians or network buffers would
+ * spill or not fit). */
+template <int NV, bool WARM, int OCC = 2, bool STAGE = false>
 __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
     const DevEphem& E = *Ep;
@@ -569,6 +675,9 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
     AgCoopTab& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
     extern __shared__ __align__(16) unsigned char ag_dyn_smem[];
+    AgRecStage* const R =
+        STAGE ? reinterpret_cast<AgRecStage*>(ag_dyn_smem + AgCoopDyn<NV, WARM, STAGE>::stage_off) : nullptr;
+    AgStageCursor cur;
     constexpr bool wss = AgCoopDyn<NV, WARM>::ws_shared;
     const Ws<C> W{wss ? reinterpret_cast<double*>(ag_dyn_smem + AgCoopDyn<NV, WARM>::warm) : A.ws,
                   wss ? 32 : A.nslots, wss ? lane : slot};
@@ -577,11 +686,13 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
     if (tid == 0) {
         for (int k = 0; k < (NV == 0 ? 8 : 1); k++) S.tab[k].T.status = AG_OK;
         S.stop = 0;
+        S.stage_fail = 0;
+        if (STAGE) ag_mbar_init(&R->bar);
     }
-    /* learned warm start and step logging (no variational particles) */
+    /* learned warm start and step logging */
     AgWarmSmem& WS = *reinterpret_cast<AgWarmSmem*>(ag_dyn_smem);
-    const bool warm = WARM && NV == 0 && A.mlp != nullptr;
-    const bool logp = WARM && NV == 0 && A.log_x != nullptr;
+    const bool warm = WARM && A.mlp != nullptr;
+    const bool logp = WARM && A.log_x != nullptr;
 
     while (true) {
         __syncthreads();
@@ -590,9 +701,9 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
         const int g = S.g;
         if (g >= A.n_groups) break;
         const int gs = A.grp_size[g], g0 = A.grp_start[g];
-        if (S.stop) {
-            /* run-time budget spent: groups still queued are not integrated
-             * (state untouched) and say so */
+        if (S.stop || S.stage_fail) {
+            /* run-time budget spent (or a record copy lost): groups still
+             * queued are not integrated (state untouched) and say so */
             if (wid == 0 && lane < gs) {
                 const int p = A.order[g0 + lane];
                 if (A.status) A.status[p] = AG_ST_TIMEOUT;
@@ -642,8 +753,16 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
         const bool dense = NV == 0 && A.out_start != nullptr;
         int on = 0, on_end = 0;
         if (dense && live) { on = A.out_start[pid]; on_end = A.out_start[pid + 1]; }
-        /* warm start per lane: on until its learned starts converge slower than
-         * the plain predictor's (every 8th step is a plain probe) */
+        /* warm start per group: on until its learned steps take longer than
+         * its plain probes (every 8th step), timed by thread 0 with clock64
+         * from the step's first body table to its converged corrector: the
+         * inference's cost against the iterations it saves, where the group
+         * iterates until its slowest member has converged */
+        long long wg_t_l = 0, wg_t_p = 0, clk_step = 0;
+        int wg_n_l = 0, wg_n_p = 0;
+        if (tid == 0) S.wg_off = 0;
+        /* and per member: on until its learned starts converge in more
+         * iterations than its plain probes */
         bool wl_on = warm;
         int wl_sum_l = 0, wl_n_l = 0, wl_sum_p = 0, wl_n_p = 0;
         while (true) {
@@ -685,7 +804,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             }
             if (!__any_sync(AG_FULL, live)) break;
             /* ---- watchdog (thread 0 decides for the block) */
-            if (tid == 0 && A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles) S.stop = 1;
+            if (tid == 0 && (S.stage_fail || (A.watchdog_cycles > 0 && clock64() - clk0 > A.watchdog_cycles))) S.stop = 1;
             __syncthreads();
             if (S.stop) {
                 pstat = AG_ST_TIMEOUT;
@@ -702,13 +821,14 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             const bool last = live && last_group && rem == rem_min;
 
             /* ---- node 0: accelerations at the step start, g from the predicted b */
-            int bad = ag_coop_table_pass1(E, cf, t, S.scr, Tab, tid);
+            if (WARM && tid == 0) clk_step = clock64();
+            int bad = ag_coop_table_pass1<STAGE>(E, cf, t, S.scr, Tab, tid, R, cur, &S.stage_fail);
             n_tab++;
             if (live)
                 for (int comp = 0; comp < C; comp++)
                     if (ag_coop_owner<NV>(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
             bad = __syncthreads_or(bad);
-            if (bad) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            if (bad) { pstat = S.stage_fail ? AG_ST_TIMEOUT : AG_ST_COVERAGE; finish_now = live; continue; }
             ag_coop_table_pass2(E, cf, t, Tab, S.scr, tid);
             __syncthreads();
             if (cf.geocentric == 1) { ag_coop_rel_geo(E, Tab, tid); __syncthreads(); }
@@ -761,10 +881,13 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                 }
             }
             /* ---- learned warm start: features, BF16 inference, b += kappa y */
-            bool w_applied = false, w_probe = false;
-            if (warm || logp)
-                ag_coop_warm_start(A, W.w, W.ns, W.slot, WS, Tab.T, lane, wid, live, warm, wl_on, hstep, dtls, steps,
-                                   w_applied, w_probe, n_wused, n_wfall);
+            bool w_applied = false, w_probe = false, w_ran = false;
+            if constexpr (WARM) {
+                if (warm || logp)
+                    w_ran = ag_coop_warm_start<NV>(A, W.w, W.ns, W.slot, WS, Tab.T, lane, wid, live, warm,
+                                                   wl_on && S.wg_off == 0, hstep, dtls, steps, w_applied, w_probe,
+                                                   n_wused, n_wfall);
+            }
             if (live) {
                 for (int comp = 0; comp < C; comp++) {
                     if (ag_coop_owner<NV>(comp) != wid) continue;
@@ -791,7 +914,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                     const double tn = t + (tc + hstep * hn);
                     AgCoopTab& TabN = S.tab[NV == 0 ? n : 0];
                     const bool build = NV != 0 || iters == 1;     /* block-uniform */
-                    bad = build ? ag_coop_table_pass1(E, cf, tn, S.scr, TabN, tid) : 0;
+                    bad = build ? ag_coop_table_pass1<STAGE>(E, cf, tn, S.scr, TabN, tid, R, cur, &S.stage_fail) : 0;
                     n_tab += build ? 1 : 0;
                     if (!conv) {
                         double sx[9], sv[8];
@@ -898,16 +1021,29 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                 if (__all_sync(AG_FULL, conv)) break;
                 iters++;
             }
-            if (cov) { pstat = AG_ST_COVERAGE; finish_now = live; continue; }
+            if (cov) { pstat = S.stage_fail ? AG_ST_TIMEOUT : AG_ST_COVERAGE; finish_now = live; continue; }
             if (warm && live) {
                 if (w_applied) { wl_sum_l += it_lane; wl_n_l++; }
                 else if (w_probe) {
                     wl_sum_p += it_lane; wl_n_p++;
-                    /* the plain predictor converges faster for this particle: fall back */
+                    /* the plain predictor converges faster for this member: fall back */
                     if (wl_n_p >= 4 && wl_n_l >= 8 && (long long)wl_sum_l * wl_n_p > (long long)wl_sum_p * wl_n_l) {
                         wl_on = false;
                         if (wid == 0) n_wfall++;
                     }
+                }
+            }
+            if (warm && !A.warm_no_time_fallback && tid == 0 && S.wg_off == 0) {
+                /* the step so far: body tables, forces, the start, the corrector */
+                const long long dt_clk = clock64() - clk_step;
+                const bool probe = (steps & 7) == 7;
+                if (w_ran) { wg_t_l += dt_clk; wg_n_l++; }
+                else if (probe) { wg_t_p += dt_clk; wg_n_p++; }
+                /* the group's learned steps take longer than its plain probes: the
+                 * plain predictor for the rest of the group */
+                if (wg_n_p >= 3 && wg_n_l >= 12 && (double)wg_t_l / wg_n_l > (double)wg_t_p / wg_n_p) {
+                    S.wg_off = 1;
+                    n_wfall++;
                 }
             }
             /* ---- step-size control: each lane's choice, the group takes the smallest */
@@ -1088,39 +1224,53 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
         atomicAdd(&A.counters[5], n_wfall);
         if (tid == 0) atomicAdd(&A.counters[6], n_tab);   /* body tables, one per block and node time */
     }
+    /* a copy that did not complete in time: wait for it once more (bounded)
+     * before the block's shared memory is released */
+    if (STAGE && tid == 0 && S.stage_fail) ag_mbar_wait(&R->bar, cur.phase ^ 1u);
 }
 
 /* Opt the kernel in to its dynamic shared memory (above the 48 KB default). */
-template <int NV, bool WARM, int OCC>
+template <int NV, bool WARM, int OCC, bool STAGE = false>
 static int ag_coop_dyn_attr() {
-    if (AgCoopDyn<NV, WARM>::bytes == 0) return 0;
-    return (int)cudaFuncSetAttribute(ag_k_coop<NV, WARM, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)AgCoopDyn<NV, WARM>::bytes);
+    if (AgCoopDyn<NV, WARM, STAGE>::bytes == 0) return 0;
+    return (int)cudaFuncSetAttribute(ag_k_coop<NV, WARM, OCC, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)AgCoopDyn<NV, WARM, STAGE>::bytes);
 }
 
-/* Slots (32 per resident block) of the plain (nv = 0, occ 2 or 3) or
- * variational (nv = 6) kernel on the current device. */
-int ag_coop_max_slots(int nv, int occ) {
+template <int NV, bool WARM, int OCC, bool STAGE = false>
+static int ag_coop_blocks_per_sm() {
+    int bps = 0;
+    if (ag_coop_dyn_attr<NV, WARM, OCC, STAGE>() == 0)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<NV, WARM, OCC, STAGE>, 128,
+                                                      AgCoopDyn<NV, WARM, STAGE>::bytes);
+    return bps;
+}
+
+/* Slots (32 per resident block) of the plain (nv = 0: occ 2 or 3, stage
+ * only with occ 2) or variational (nv = 6) kernel, or of their learned
+ * warm-start builds (warm), on the current device. */
+int ag_coop_max_slots(int nv, int occ, int stage, int warm) {
     int dev = 0, sms = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (nv == 6) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<6, false, 2>, 128, AgCoopDyn<6, false>::bytes);
-    } else if (occ == 3) {
-        if (ag_coop_dyn_attr<0, false, 3>() == 0)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false, 3>, 128, AgCoopDyn<0, false>::bytes);
-    } else if (ag_coop_dyn_attr<0, false, 2>() == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ag_k_coop<0, false, 2>, 128, AgCoopDyn<0, false>::bytes);
-    }
+    if (nv == 6) bps = warm ? ag_coop_blocks_per_sm<6, true, 2>() : ag_coop_blocks_per_sm<6, false, 2>();
+    else if (warm) bps = ag_coop_blocks_per_sm<0, true, 2>();
+    else if (occ == 3) bps = ag_coop_blocks_per_sm<0, false, 3>();
+    else if (stage) bps = ag_coop_blocks_per_sm<0, false, 2, true>();
+    else bps = ag_coop_blocks_per_sm<0, false, 2>();
     if (bps < 1) bps = 1;
     return sms * bps * 32;
 }
 
-int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, cudaStream_t s) {
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, int stage,
+                   cudaStream_t s) {
     int e = ag_ias_tables_init();
     if (e) return e;
     const int blocks = (a.nslots + 31) / 32;
-    if (nv == 6) {
+    if (nv == 6 && (a.mlp || a.log_x)) {
+        if ((e = ag_coop_dyn_attr<6, true, 2>())) return e;
+        ag_k_coop<6, true, 2><<<blocks, 128, AgCoopDyn<6, true>::bytes, s>>>(E.self_dev, c, a);
+    } else if (nv == 6) {
         ag_k_coop<6, false, 2><<<blocks, 128, AgCoopDyn<6, false>::bytes, s>>>(E.self_dev, c, a);
     } else if (a.mlp || a.log_x) {
         if ((e = ag_coop_dyn_attr<0, true, 2>())) return e;
@@ -1128,9 +1278,25 @@ int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, i
     } else if (occ == 3) {
         if ((e = ag_coop_dyn_attr<0, false, 3>())) return e;
         ag_k_coop<0, false, 3><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
+    } else if (stage) {
+        if ((e = ag_coop_dyn_attr<0, false, 2, true>())) return e;
+        ag_k_coop<0, false, 2, true><<<blocks, 128, AgCoopDyn<0, false, true>::bytes, s>>>(E.self_dev, c, a);
     } else {
         if ((e = ag_coop_dyn_attr<0, false, 2>())) return e;
         ag_k_coop<0, false, 2><<<blocks, 128, AgCoopDyn<0, false>::bytes, s>>>(E.self_dev, c, a);
     }
     return (int)cudaGetLastError();
+}
+
+/* What a launch of this kernel sets up on its first use on a device (the
+ * IAS15 tables, the shared-memory opt-ins of every build), done ahead of a
+ * stream capture. */
+int ag_coop_ready(void) {
+    int e = ag_ias_tables_init();
+    if (!e) e = ag_coop_dyn_attr<0, false, 2>();
+    if (!e) e = ag_coop_dyn_attr<0, false, 3>();
+    if (!e) e = ag_coop_dyn_attr<0, false, 2, true>();
+    if (!e) e = ag_coop_dyn_attr<0, true, 2>();
+    if (!e) e = ag_coop_dyn_attr<6, true, 2>();
+    return e;
 }

@@ -49,6 +49,7 @@ struct AgBatchArgs {
     int n_groups;
     /* learned warm start (block-cooperative kernel, no variational particles) */
     const struct AgMlpDev* mlp;     /* network for the warm start, or null (plain predictor) */
+    int warm_no_time_fallback;      /* keep the learned start in groups where it costs time */
     float* log_x;                   /* [log_cap][32] features of logged steps, or null */
     float* log_t;                   /* [log_cap][21] their targets */
     int* log_count;                 /* next log row (atomic) */
@@ -71,14 +72,18 @@ int ag_launch_batch(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, 
 int ag_batch_max_slots(int nv, int tpb);
 int ag_group_max_slots(int nv);
 int ag_launch_group(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, cudaStream_t s);
-int ag_coop_max_slots(int nv, int occ);
+int ag_coop_max_slots(int nv, int occ, int stage, int warm);
 /* Per-particle encounter cost ratio (extra steps / base steps) from a
  * two-body pilot on a G-point time grid over [tmin, tmax]. */
 int ag_pilot_encounters(const DevEphem& E, int n, const double* d_t0, const double* d_te, const double* d_state,
                         double tmin, double tmax, float* d_ratio, float4* d_grid, float2* d_sunv, int G,
                         cudaStream_t s);
-int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, cudaStream_t s);
+int ag_launch_coop(const DevEphem& E, const ForceCfg& c, const AgBatchArgs& a, int nv, int occ, int stage,
+                   cudaStream_t s);
 double ag_fp64_probe_gflops(void);
+/* first-use set-up of the batched kernels (tables, shared-memory opt-ins), ahead of a stream capture */
+int ag_batch_ready(void);
+int ag_coop_ready(void);
 
 /* shared-step device IAS15 (kernels_shared.cu) */
 struct AgSharedSim;
@@ -92,12 +97,24 @@ struct assist_ephem;
 /* The device view of an ephemeris (uploaded on first use). */
 int ag_ephem_device(const struct assist_ephem* e, DevEphem* out);
 
+/* The device view of an ephemeris that already has one matching its current
+ * contents, without allocating or uploading anything (an error otherwise). */
+int ag_ephem_device_current(const struct assist_ephem* e, DevEphem* out);
+
 /* 1 when the ephemeris's device view exists (ag_ephem_device will not allocate) */
 int ag_ephem_view_ready(const struct assist_ephem* e);
 
 /* warm-start network (kernels_mlp.cu) */
 const struct AgMlpDev* ag_mlp_device_view(void);
 int ag_mlp_log_config(float** x, float** t, int* cap, int* every, int** count);
+
+/* build selection of the block-cooperative kernel (autotune.cpp): a batch's
+ * signature, the recorded build for it (0 none; 2, 3 blocks per SM; 4 two
+ * with the staged record) and the signature of the last batch formed */
+std::string ag_tune_key(int n_groups, int n, const double* t0, const double* te, const unsigned char* has_ng,
+                        int forces, int gr_eih_sources, int geocentric, int planets_spk);
+int ag_tune_lookup(const std::string& key);
+void ag_tune_note(const std::string& key);
 
 /* library error state */
 void ag_set_error(const std::string& msg);

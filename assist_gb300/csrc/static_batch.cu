@@ -81,22 +81,28 @@ extern "C" int assist_gb300_integrate_batch_device_static(const struct assist_ep
                                                          const double* d_params, int* d_status, void* stream,
                                                          struct assist_gb300_batch_stats* stats) {
     if (!o) { ag_set_error("options are required"); return ASSIST_ERROR_N; }
-    if (n < 0 || n > ASSIST_GB300_STATIC_MAX_PARTICLES) {
+    if (n < 0) {
+        ag_set_error("static-scratch batch: the particle count must not be negative");
+        return ASSIST_ERROR_N;
+    }
+    if (n > ASSIST_GB300_STATIC_MAX_PARTICLES) {
         char msg[160];
         std::snprintf(msg, sizeof(msg), "static-scratch batch: %d particles requested, at most %d fit in its %d MiB scratch",
                       n, ASSIST_GB300_STATIC_MAX_PARTICLES, ASSIST_GB300_STATIC_SCRATCH_BYTES >> 20);
         ag_set_error(msg);
         return ASSIST_ERROR_N;
     }
+    if (o->warm_start) {
+        ag_set_error("static-scratch batch: the learned warm start needs the allocating entry points");
+        return ASSIST_ERROR_N;
+    }
     if (n == 0) { if (stats) std::memset(stats, 0, sizeof(*stats)); return ASSIST_SUCCESS; }
     if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
-    if (!ag_ephem_view_ready(e)) {
-        ag_set_error("static-scratch batch: the ephemeris has no device view yet; make one ordinary device call "
-                     "(e.g. assist_gb300_integrate_batch_device) with it first");
-        return ASSIST_ERROR_EPHEM_FILE;
-    }
+    /* the ephemeris's device view as it stands: this path neither allocates
+     * nor uploads one (an ephemeris edited since its last ordinary device
+     * call is refused) */
     DevEphem D;
-    int st = ag_ephem_device(e, &D);
+    int st = ag_ephem_device_current(e, &D);
     if (st) return st;
     unsigned char* scratch = nullptr;
     if (ag_static_scratch_address(&scratch)) return ASSIST_ERROR_EPHEM_FILE;

@@ -86,14 +86,14 @@ __device__ __forceinline__ int ag_astcomp_exact(const DevEphem& E, int m, int co
 
 /* Velocity of a further EIH source, or of the geocentric Earth (rare
  * configurations; kept out of line). */
-__device__ __noinline__ void ag_table_velocity(const DevEphem& E, const double* rec, double tf, int body, AgTable& T) {
+static __device__ __noinline__ void ag_table_velocity(const DevEphem& E, const double* rec, double tf, int body, AgTable& T) {
     double u[3], v[3];
     ag_planet_exact<true>(E, rec, tf, body, u, v);
     T.P.vx[body] = v[0]; T.P.vy[body] = v[1]; T.P.vz[body] = v[2];
 }
 
 /* Earth's barycentric acceleration for the geocentric frame. */
-__device__ __noinline__ void ag_table_earth_acc(const DevEphem& E, double t, AgTable& T) {
+static __device__ __noinline__ void ag_table_earth_acc(const DevEphem& E, double t, AgTable& T) {
     double e_[10];
     ag_planet_full(E, AG_EAR, t, e_);
     T.P.ex_a[0] = e_[7]; T.P.ex_a[1] = e_[8]; T.P.ex_a[2] = e_[9];
@@ -145,7 +145,7 @@ __device__ __forceinline__ int ag_warp_table_rest(const DevEphem& E, const Force
 
 /* The planets of the table from a planets SPK file: one lane per body, full
  * state (src/spk.c:550-608).  Returns a warp-uniform status. */
-__device__ __noinline__ int ag_warp_planets_spk(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
+static __device__ __noinline__ int ag_warp_planets_spk(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, int lane) {
     int st = AG_OK;
     if (lane < AG_NPL) {
         double o[10];
@@ -161,7 +161,7 @@ __device__ __noinline__ int ag_warp_planets_spk(const DevEphem& E, const ForceCf
 /* Build the table of time t with the whole warp.  Returns a warp-uniform
  * status.  Falls back to body-per-lane velocities when more EIH sources than
  * the Sun need velocities (rare configuration). */
-__device__ __noinline__ int ag_warp_table_fast(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, AgWarpScratch& S,
+static __device__ __noinline__ int ag_warp_table_fast(const DevEphem& E, const ForceCfg& c, double t, AgTable& T, AgWarpScratch& S,
                                   int lane) {
     if (E.pl_spk) {
         const int sp = ag_warp_planets_spk(E, c, t, T, lane);

@@ -406,17 +406,40 @@ def main():
                      "loss_initial": l0, "loss_final": loss, "train_s": time.perf_counter() - t}
         del X, T
 
-    # the learned warm start, measured beside the plain predictor (the default path)
+    # build selection (outside every timed region): the autotuner times the
+    # default kernel's builds on this batch and records the fastest, which
+    # the automatic mode then uses; with the learned warm start requested it
+    # also times the learned build against them
+    tune = batch.autotune_device(eph, t0, te, st0, params=prm, opts=opts) if args.blocks_per_sm == 0 else None
+    tune_warm = None
+    if not args.no_warm:
+        tune_warm = batch.autotune_device(eph, t0, te, st0, params=prm, opts=warm_opts)
+
+    def learned_line(o, steps, warmup):
+        lms, lacc, lstat_, lst_, _, _ = timed_batch(batch, eph, t0, te, st0, prm, o, steps, warmup, stream, flush,
+                                                    world, dist=dist)
+        ldone = lstat_ == 0
+        d = {"value": world * float(np.abs(pop.t_end - pop.t0)[ldone].sum()) * steps / (lms / 1e3),
+             "unit": UNIT, "ms_per_step": lms / steps, "steps": steps, "warmup": warmup,
+             "iterations_per_step": lacc["pc_iterations"] / max(lacc["steps_accepted"] + lacc["steps_rejected"], 1),
+             "force_evals": lacc["force_evals"] // steps,
+             "used": lacc["warm_start_used"] // steps, "fallback": lacc["warm_start_fallback"] // steps}
+        return d, lstat_, lst_
+
+    # the learned warm start, measured beside the plain predictor (the default
+    # path): warm_start = 1 (learned unless the autotuner found the plain
+    # predictor faster on this batch; groups and members fall back on their
+    # own), then the learned build regardless (2) and on every step without
+    # the time test (3), the last two as diagnostics over fewer steps
     learned, lstat, lst = None, None, None
     if not args.no_warm:
-        lms, lacc, lstat, lst, _, _ = timed_batch(batch, eph, t0, te, st0, prm, warm_opts, args.steps, args.warmup,
-                                                  stream, flush, world, dist=dist)
-        ldone = lstat == 0
-        learned = {"value": world * float(np.abs(pop.t_end - pop.t0)[ldone].sum()) * args.steps / (lms / 1e3),
-                   "unit": UNIT, "ms_per_step": lms / args.steps,
-                   "iterations_per_step": lacc["pc_iterations"] / max(lacc["steps_accepted"] + lacc["steps_rejected"], 1),
-                   "force_evals": lacc["force_evals"] // args.steps,
-                   "used": lacc["warm_start_used"] // args.steps, "fallback": lacc["warm_start_fallback"] // args.steps}
+        learned, lstat, lst = learned_line(warm_opts, args.steps, args.warmup)
+        learned["mode"] = "warm_start=1: learned unless the autotuner recorded the plain predictor faster"
+        learned["autotune"] = tune_warm
+        forced, _, _ = learned_line(batch.options(group_steps=2, warm_start=2), min(args.steps, 2), 1)
+        every, _, _ = learned_line(batch.options(group_steps=2, warm_start=3), min(args.steps, 2), 1)
+        learned["learned_build_forced"] = forced
+        learned["every_step_no_time_test"] = every
     clocks = ClockSampler(local)
     clocks.start()
     ms, stats_acc, st_host, st_end, _, wall = timed_batch(batch, eph, t0, te, st0, prm, opts, args.steps, args.warmup,
@@ -432,6 +455,8 @@ def main():
         both = done & (lstat == 0)
         d = np.abs(st_end[both, :3] - lst[both, :3]).max(axis=1)
         learned["ratio_to_plain"] = learned["value"] / value
+        learned["learned_build_forced"]["ratio_to_plain"] = learned["learned_build_forced"]["value"] / value
+        learned["every_step_no_time_test"]["ratio_to_plain"] = learned["every_step_no_time_test"]["value"] / value
         learned["end_state_vs_plain_au"] = {"median": float(np.median(d)), "max": float(d.max()),
                                             "particles_over_1e-9": int((d > 1e-9).sum()),
                                             "status_mismatches": int((st_host != lstat).sum())}
@@ -452,6 +477,30 @@ def main():
         d2h = pop.state.nbytes + hstat.nbytes
         e2e = {"value": e2e_days / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "calls": args.steps, "ms_per_call": 1e3 * e2e_s / args.steps}
+    # the same batch as a plan: host work once, each step a CUDA-graph replay
+    graph = None
+    if rank == 0:
+        gst = st0.clone()
+        gstat = torch.zeros(N_PARTICLES, dtype=torch.int32, device=dev)
+        plan = batch.Plan(eph, t0, te, gst, params=prm, status=gstat, opts=opts, stream=stream)
+        gms = 0.0
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1.0)
+            gst.copy_(st0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.launch(stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                gms += e0.elapsed_time(e1)
+        gstats = plan.stats()
+        plan.close()
+        same = bool(torch.equal(gst.cpu(), torch.tensor(st_end)))
+        graph = {"value": pdays * args.steps / (gms / 1e3), "unit": UNIT, "ms_per_step": gms / args.steps,
+                 "force_evals": gstats["force_evals"], "end_states_equal_direct_call": same,
+                 "note": "assist_gb300_plan_*: grouping once, each step a CUDA-graph replay of the device work"}
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -512,7 +561,8 @@ def main():
             "clocks": clocks.summary(),
             "ias15": ias15_summary(stats_acc, args.steps),
             "unfinished_particles": int((~done).sum()), "status_counts": status_counts,
-            "wall_s_timed_region": wall, "learned_warm_start": learned, "configs": configs}
+            "wall_s_timed_region": wall, "learned_warm_start": learned, "autotune": tune, "graph_replay": graph,
+            "configs": configs}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -202,8 +202,16 @@ struct assist_gb300_options {
     double dt0;             /* initial |dt| (REBOUND default 0.001 day) */
     int max_steps;          /* per-particle step budget, 0 => unlimited */
     int warm_start;         /* 0 plain predictor; 1 learned warm start (needs a network, see
-                               assist_gb300_warm_*; group_steps = 2 and no variational particles) */
-    int threads_per_block;  /* 0 => autotuned */
+                               assist_gb300_warm_*; group_steps = 2), except for batches whose
+                               signature assist_gb300_autotune_device recorded the plain predictor
+                               faster on; 2 learned warm start regardless.  Every 8th step of a
+                               group is a plain probe; a member whose learned starts converge in
+                               more iterations than its probes, and a group whose learned steps
+                               take longer than its probes, fall back to the plain predictor.
+                               3: as 2 without the group's time test (what the network saves in
+                               iterations, whatever it costs) */
+    int threads_per_block;  /* group_steps 0: 0 => 128, halved (down to 32) while the batch would
+                               leave SMs idle */
     int group_steps;        /* 1: up to 32 particles with the same start time and similar
                                orbital timescale share each adaptive step (one warp);
                                2 (default): the same groups, each integrated by a 128-thread
@@ -218,6 +226,11 @@ struct assist_gb300_options {
     int blocks_per_sm;      /* group_steps 2 without variational particles or warm start:
                                0 (default) three resident blocks per SM when the batch has at
                                least 8 groups per such block, else two; 2 or 3 force it */
+    int ephem_staging;      /* group_steps 2 without variational particles or warm start, .440
+                               planets: 0 (default) the library's choice; 1 each block keeps its
+                               group's active .440 record in shared memory, staged by bulk (TMA)
+                               copies (two resident blocks per SM); 2 coefficients read from
+                               global memory */
 };
 
 /* Fill `opt` with ASSIST's defaults (src/assist.c:408-447). */
@@ -297,8 +310,14 @@ int assist_gb300_integrate_batch_dense_device(const struct assist_ephem* ephem, 
  * synchronisation of cudaFree.  Its scratch (queue, counters, workspace) is
  * one fixed __device__ array of ASSIST_GB300_STATIC_SCRATCH_BYTES per device;
  * n above ASSIST_GB300_STATIC_MAX_PARTICLES is rejected with
- * ASSIST_ERROR_N.  The ephemeris must already have a device view (one
- * ordinary device call with it first).  The first call on a device looks up
+ * ASSIST_ERROR_N.  opt->group_steps is ignored (always independent steps);
+ * warm_start must be 0.  Particles are taken in index order (the
+ * allocating entry point queues the longest integrations first), which can
+ * leave a long integration near the end of a large batch running alone.
+ * The ephemeris must already have a device view that matches its current
+ * contents (one ordinary device call with it first, and again after editing
+ * jd_ref or a constant): this entry point neither allocates nor uploads one
+ * and refuses a stale one.  The first call on a device looks up
  * the scratch address and uploads the IAS15 tables: make it before any stream
  * capture.  One scratch per device: calls that overlap in time on one device
  * (other streams or threads) race on it and must be serialised by the caller.
@@ -310,6 +329,59 @@ int assist_gb300_integrate_batch_device_static(const struct assist_ephem* ephem,
                                                const double* d_t0, const double* d_t_end, double* d_state,
                                                const double* d_params, int* d_status, void* stream,
                                                struct assist_gb300_batch_stats* stats);
+
+/* Plans: one batch integrated repeatedly (no counterpart in the reference).
+ * assist_gb300_plan_create does the host work of an assist_gb300_integrate_
+ * batch_device call once -- inputs read back, encounter pilot, grouping, the
+ * kernel build -- from the arrays' current contents, and captures the device
+ * work (queue and counter reset, the persistent kernel, the counters' copy
+ * to host memory) as a CUDA graph.  Each assist_gb300_plan_launch replays it
+ * on `stream` over the same device arrays: write the next initial states
+ * (and times, if they keep the grouping's meaning) into them between
+ * launches.  A replay gives the result of a direct call whose grouping is
+ * the plan's (bit for bit when the inputs are the ones the plan was made
+ * from).  No dense output or pair logging.  assist_gb300_plan_stats waits
+ * for the last launch and returns its counters (kernel_ms -1: time launches
+ * with events on their stream).  A plan belongs to the device that was
+ * current at its creation. */
+struct assist_gb300_plan;
+int assist_gb300_plan_create(const struct assist_ephem* ephem, const struct assist_gb300_options* opt, int n,
+                             const double* d_t0, const double* d_t_end, double* d_state, const double* d_params,
+                             int n_var, double* d_var_state, int* d_status, void* stream,
+                             struct assist_gb300_plan** plan);
+int assist_gb300_plan_launch(struct assist_gb300_plan* plan, void* stream);
+int assist_gb300_plan_stats(struct assist_gb300_plan* plan, struct assist_gb300_batch_stats* stats);
+void assist_gb300_plan_free(struct assist_gb300_plan* plan);
+
+/* Build selection of the default batched kernel (no counterpart in the
+ * reference).  The block-cooperative kernel (group_steps = 2) without
+ * variational particles has three builds that compute the same results: two
+ * or three resident blocks per SM, and two with each block's active .440
+ * record staged in shared memory by bulk copies.  This times each on the
+ * caller's batch (device arrays; the state is copied, not changed), reports
+ * the kernel times and records the fastest for the batch's signature
+ * (device, group count, mean and longest length, non-gravitational share,
+ * force model, planets format) in memory and in the file named by
+ * ASSIST_GB300_TUNE_CACHE (default ~/.cache/assist_gb300/tune.txt; empty:
+ * memory only).  Later calls with blocks_per_sm = 0 and ephem_staging = 0
+ * use the recorded build for a batch of the same signature.  With
+ * warm_start set in `opt` the learned warm-start build is a candidate too
+ * (with variational particles: the plain and the learned build), and
+ * warm_start = 1 calls use the plain predictor on batches of a signature
+ * where it was faster.  It allocates scratch for a copy of the state (and of
+ * d_var_state) and runs the batch twice per build. */
+struct assist_gb300_tune_result {
+    int chosen;              /* 2, 3: plain, blocks per SM; 4: plain, two with the staged .440
+                                record; 5: the learned warm start */
+    int n_candidates;
+    int candidate[4];
+    double kernel_ms[4];     /* best of two kernel times of each candidate */
+    char signature[512];
+};
+int assist_gb300_autotune_device(const struct assist_ephem* ephem, const struct assist_gb300_options* opt, int n,
+                                 const double* d_t0, const double* d_t_end, const double* d_state,
+                                 const double* d_params, int n_var, const double* d_var_state, void* stream,
+                                 struct assist_gb300_tune_result* result);
 
 /* ---- Learned IAS15 warm start (no counterpart in the reference).
  * One network per process: 32 step features -> 256 -> 256 -> 21 corrections

@@ -1569,6 +1569,94 @@ int orc_integrate_cb(orc_force_cb cb, void* ctx, double t0, double t_end, int N,
     return r;
 }
 
+/* Warm-start ceiling study (test infrastructure: what any predictor of
+ * IAS15's b can save).  Particles are integrated in shared-step groups of
+ * `group` consecutive particles (group = 1: independent steps; the group's
+ * error and convergence measures are maxima over its members, as in a
+ * kernel whose members share each step), each group from t0[first] to
+ * t_end[first].  At every accepted step the step is replayed from its saved
+ * start with the predictor's b replaced by b_conv (1 + rel_err[k] u), u
+ * uniform in [-1, 1] per coefficient (seeded), for each of the n_err
+ * relative errors (0: the converged b itself), and the replay's
+ * predictor-corrector iterations are tallied.  hist: (1 + n_err) rows of 13
+ * counts of accepted steps by iterations, row 0 the plain predictor's. */
+int orc_warm_start_study(void* h, int fbits, int gr_eih_sources, int geocentric, const double* law, int n,
+                         int group, const double* t0, const double* t_end, const double* state, const double* params,
+                         double epsilon, double dt0, double dt_floor, int threads, int n_err, const double* rel_err,
+                         unsigned long long seed, long long* hist) {
+    if (group < 1 || n_err < 0 || n_err > 16) return -1;
+    const int ng = (n + group - 1) / group;
+    std::atomic<int> next(0);
+    std::vector<long long> H((size_t)(1 + n_err) * 13 * (size_t)(threads > 0 ? threads : 1), 0);
+    auto work = [&](int tid) {
+        long long* Ht = H.data() + (size_t)tid * (1 + n_err) * 13;
+        OracleForces<double> F;
+        F.e = (Ephem*)h; F.o = mkopts(fbits, gr_eih_sources, geocentric, law); F.n_var = 0;
+        IasOpts io{epsilon, 0.0, 0, 12, dt_floor};
+        uint64_t rs = seed * 0x9E3779B97F4A7C15ull + 1 + (uint64_t)tid;
+        auto uni = [&]() {     /* xorshift64*, uniform in [-1, 1] */
+            rs ^= rs >> 12; rs ^= rs << 25; rs ^= rs >> 27;
+            return (double)((rs * 0x2545F4914F6CDD1Dull) >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        };
+        while (true) {
+            const int g = next.fetch_add(1);
+            if (g >= ng) break;
+            const int i0 = g * group, m = std::min(group, n - i0);
+            F.n_real = m;
+            F.vtp.clear();
+            std::vector<double> prm;
+            F.params = nullptr;
+            if (params) { prm.assign(params + 3 * (size_t)i0, params + 3 * (size_t)(i0 + m)); F.params = prm.data(); }
+            Ias15<double> I(m, m);
+            for (int j = 0; j < m; j++)
+                for (int k = 0; k < 3; k++) {
+                    I.x0[3 * j + k] = state[6 * (size_t)(i0 + j) + k];
+                    I.v0[3 * j + k] = state[6 * (size_t)(i0 + j) + 3 + k];
+                }
+            I.t = t0[i0]; I.dt = dt0;
+            const double te = t_end[i0];
+            const double dir = te - I.t >= 0 ? 1.0 : -1.0;
+            if (I.dt * dir <= 0) I.dt = std::fabs(I.dt) * dir;
+            IasStats st{0, 0, 0, 0, 0};
+            while (I.t != te) {
+                const double rem = (te - I.t) - I.tc;
+                bool last = false;
+                double hs = I.dt;
+                if (std::fabs(I.dt) >= std::fabs(rem)) { hs = rem; last = true; }
+                Ias15<double> S0 = I;
+                const long long it0 = st.iterations;
+                double dtn;
+                const int r = I.step(F, hs, io, st, &dtn, last);
+                if (r < 0 || r == 2) break;
+                if (r == 1) {
+                    Ht[std::min<long long>(st.iterations - it0, 12)]++;
+                    for (int q = 0; q < n_err; q++) {
+                        Ias15<double> R = S0;
+                        for (int k = 0; k < 7; k++)
+                            for (size_t c = 0; c < R.b[k].size(); c++) R.b[k][c] = I.br[k][c] * (1.0 + rel_err[q] * uni());
+                        IasStats sr{0, 0, 0, 0, 0};
+                        double dtr;
+                        R.step(F, hs, io, sr, &dtr, last);
+                        Ht[(size_t)(1 + q) * 13 + std::min<long long>(sr.iterations, 12)]++;
+                    }
+                }
+                I.dt = dtn;
+                if (r == 1 && last) { I.t = te; I.tc = 0.0; }
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    for (int k = 1; k < threads; k++) pool.emplace_back(work, k);
+    work(0);
+    for (auto& th : pool) th.join();
+    for (size_t k = 0; k < (size_t)(1 + n_err) * 13; k++) {
+        hist[k] = 0;
+        for (int t = 0; t < threads; t++) hist[k] += H[(size_t)t * (1 + n_err) * 13 + k];
+    }
+    return 0;
+}
+
 /* Batched independent particles: particle i (with n_var_each variational
  * particles, 0 or 6) is its own simulation from t0[i] to t_end[i].
  * state: n*6; var_state: n*n_var_each*6; params: n*3 rows for the real

@@ -39,6 +39,8 @@ def load_lib():
     lib.orc_forces.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, C.c_int, D, D, C.c_int, I, D, D, D, D]
     lib.orc_forces_dd.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, C.c_int, D, D, C.c_int, I, D, D,
                                   D, D, D]
+    lib.orc_warm_start_study.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_int, C.c_int, D, D, D, D,
+                                         C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, D, C.c_ulonglong, L]
     lib.orc_count_ops.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, D, D, C.c_int, D, D, D, L]
     lib.orc_integrate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, D, C.c_double, C.c_double, C.c_int, C.c_int, I,
                                   D, D, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, L, D, D]
@@ -170,6 +172,27 @@ class Oracle:
         out = buf.reshape(-1, 6)
         return out[:n], out[n:], dict(status=r, accepted=int(stats[0]), rejected=int(stats[1]), evals=int(stats[2]),
                                       iterations=int(stats[3]), t=tout.value, dt=dtout.value)
+
+    def warm_start_study(self, t0, t_end, state, rel_err, group=1, params=None, epsilon=1e-9, dt0=0.001,
+                         dt_floor=1e-8, threads=None, seed=1, forces=0x7F, gr_eih_sources=1, law=DEFAULT_LAW):
+        """Corrector iterations per accepted step of the plain predictor and
+        of replays of each step started from the converged b with relative
+        error rel_err[k] (shared-step groups of `group` particles).  Returns
+        an int array (1 + len(rel_err), 13) of step counts by iterations."""
+        st = np.ascontiguousarray(state, np.float64).reshape(-1, 6)
+        n = st.shape[0]
+        t0 = np.ascontiguousarray(np.broadcast_to(np.asarray(t0, np.float64), (n,))).copy()
+        te = np.ascontiguousarray(np.broadcast_to(np.asarray(t_end, np.float64), (n,))).copy()
+        prm = None if params is None else np.ascontiguousarray(params, np.float64).reshape(n, 3)
+        errs = np.ascontiguousarray(rel_err, np.float64)
+        hist = np.zeros((1 + errs.size, 13), np.int64)
+        law = np.asarray(law, np.float64)
+        r = self.lib.orc_warm_start_study(self.h, forces, gr_eih_sources, 0, _p(law), n, group, _p(t0), _p(te), _p(st),
+                                          _p(prm), epsilon, dt0, dt_floor, threads or os.cpu_count() or 1, errs.size,
+                                          _p(errs), seed, hist.ctypes.data_as(L))
+        if r != 0:
+            raise RuntimeError("warm-start study status %d" % r)
+        return hist
 
     def integrate_batch(self, t0, t_end, state, params=None, var_state=None, epsilon=1e-9, min_dt=0.0, dt0=0.001,
                         max_steps=0, threads=None, forces=0x7F, gr_eih_sources=1, geocentric=0, law=DEFAULT_LAW,

@@ -257,3 +257,82 @@ def test_batch_watchdog_marks_every_unfinished_particle(synth_files, monkeypatch
     if ok.size:
         ref = O.integrate_batch(pop.t0[ok], pop.t_end[ok], pop.state[ok])
         assert np.abs(out[ok, :3] - ref[:, :3]).max() < 1e-9
+
+
+def test_coop_builds_bitwise_identical(synth_files):
+    """The block-cooperative kernel's builds (two and three resident blocks
+    per SM; the .440 record staged in shared memory by bulk copies or read
+    from global memory) run each group's arithmetic identically: the same
+    end states bit for bit, the same step counts."""
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mix", 2048, seed=43, t0=8000.0, log_len=(30.0, 900.0), nongrav_frac=0.1,
+                           close_frac=0.01)
+    runs = {}
+    for name, kw in (("occ2", dict(blocks_per_sm=2, ephem_staging=2)), ("occ3", dict(blocks_per_sm=3)),
+                     ("staged", dict(ephem_staging=1))):
+        out, _, status, stats = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params,
+                                                      opts=batch.options(group_steps=2, **kw))
+        runs[name] = (out, status, stats)
+    ref = runs["occ2"]
+    for name in ("occ3", "staged"):
+        out, status, stats = runs[name]
+        assert np.array_equal(status, ref[1]), name
+        assert np.array_equal(out, ref[0]), (name, np.abs(out - ref[0]).max())
+        assert stats["steps_accepted"] == ref[2]["steps_accepted"] and stats["force_evals"] == ref[2]["force_evals"]
+
+
+def test_autotune_records_and_uses_a_build(synth_files, tmp_path, monkeypatch):
+    """The autotuner times the default kernel's builds on the batch, writes
+    its choice under the batch's signature, and an automatic-mode call of a
+    batch with that signature gives the forced builds' results."""
+    import torch
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mix", 4096, seed=44, t0=8000.0, log_len=(30.0, 600.0), nongrav_frac=0.1)
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("ASSIST_GB300_TUNE_CACHE", str(cache))
+    dev = torch.device("cuda:0")
+    t0 = torch.tensor(pop.t0, device=dev); te = torch.tensor(pop.t_end, device=dev)
+    st = torch.tensor(pop.state, device=dev); prm = torch.tensor(pop.params, device=dev)
+    r = batch.autotune_device(eph, t0, te, st, params=prm)
+    assert r["chosen"] in (2, 3, 4) and len(r["candidates_ms"]) == 3
+    assert all(v > 0 for v in r["candidates_ms"].values())
+    assert torch.equal(st, torch.tensor(pop.state, device=dev))          # the caller's state is not changed
+    assert r["signature"] in cache.read_text()
+    out, _, status, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params)
+    ref, _, rstatus, _ = batch.integrate_batch(eph, pop.t0, pop.t_end, pop.state, params=pop.params,
+                                               opts=batch.options(blocks_per_sm=2, ephem_staging=2))
+    assert np.array_equal(status, rstatus) and np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("group_steps", [0, 2])
+def test_plan_graph_replay_bitwise(synth_files, group_steps):
+    """A plan's CUDA-graph replays reproduce the direct call bit for bit
+    (same inputs, so the same grouping), launch after launch."""
+    import torch
+    from assist_gb300 import batch, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "mix", 3000, seed=45, t0=8000.0, log_len=(30.0, 600.0), nongrav_frac=0.1)
+    dev = torch.device("cuda:0")
+    t0 = torch.tensor(pop.t0, device=dev); te = torch.tensor(pop.t_end, device=dev)
+    s0 = torch.tensor(pop.state, device=dev); prm = torch.tensor(pop.params, device=dev)
+    o = batch.options(group_steps=group_steps)
+    direct = s0.clone()
+    dstat = torch.zeros(3000, dtype=torch.int32, device=dev)
+    ref_stats = batch.integrate_batch_device(eph, t0, te, direct, params=prm, status=dstat, opts=o)
+    st = s0.clone()
+    status = torch.zeros(3000, dtype=torch.int32, device=dev)
+    plan = batch.Plan(eph, t0, te, st, params=prm, status=status, opts=o)
+    for _ in range(2):
+        st.copy_(s0)
+        status.zero_()
+        plan.launch()
+        stats = plan.stats()
+        assert torch.equal(st, direct) and torch.equal(status, dstat)
+        assert stats["steps_accepted"] == ref_stats["steps_accepted"]
+        assert stats["force_evals"] == ref_stats["force_evals"]
+    plan.close()

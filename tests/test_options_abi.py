@@ -17,7 +17,7 @@ def test_default_options_fill_the_mirror_exactly():
     assert (o.alpha, o.nk, o.nm, o.nn, o.r0) == (1.0, 0.0, 2.0, 5.093, 1.0)
     assert o.epsilon == 1e-9 and o.min_dt == 0.0 and o.dt0 == 0.001 and o.max_steps == 1000000
     assert o.warm_start == 0 and o.threads_per_block == 0 and o.group_steps == 2
-    assert o.dt_floor == 1e-8 and o.group_order == 0 and o.blocks_per_sm == 0
+    assert o.dt_floor == 1e-8 and o.group_order == 0 and o.blocks_per_sm == 0 and o.ephem_staging == 0
 
 
 def test_options_keywords():

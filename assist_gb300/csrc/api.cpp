@@ -781,6 +781,9 @@ static void ag_group_keys(int n, const double* t0, const double* te, const doubl
                 tp = (te[(size_t)i] >= t0[(size_t)i]) ? (2.0 * M_PI - M) / nm : M / nm;
             }
             k.k1 = -std::floor(16.0 * std::log2(std::max(L, 1e-3)));
+            /* group_order 2: eccentricity in eighths between the length and
+             * the pericentre-time keys */
+            if (group_order == 2) k.k1 = 16.0 * k.k1 + std::floor(8.0 * std::min(std::max(ecc, 0.0), 0.999));
             k.k2 = tp;
             if (inv_a > 1e-12 && ecc < 1.0 && ecc > 1e-9 && tp > L) {
                 /* an interval shorter than half an orbit without a pericentre
@@ -828,7 +831,7 @@ static void ag_group_form(std::vector<AgGroupKey>& key, const float* ratio, int 
         for (int i = 0; i < n; i++) key[(size_t)i].cost *= 1.0 + (double)ratio[key[(size_t)i].idx];
     /* group_order 1 orders by its bucket but breaks groups only at start
      * time, direction and the non-gravitational flag */
-    const unsigned brk = group_order == 0 ? ~0u : (3u << 30);
+    const unsigned brk = group_order == 1 ? (3u << 30) : ~0u;
     std::vector<double> gl;
     int i = 0;
     while (i < n) {
@@ -865,6 +868,10 @@ static int ag_batch_validate(const struct assist_gb300_options* o, int n_var) {
     if (!o) { ag_set_error("options are required"); return ASSIST_ERROR_N; }
     if (n_var != 0 && n_var != 6) { ag_set_error("n_var must be 0 or 6"); return ASSIST_ERROR_N; }
     if (!(o->dt0 > 0) || !(o->epsilon >= 0)) { ag_set_error("dt0 must be > 0 and epsilon >= 0"); return ASSIST_ERROR_N; }
+    if (o->group_order < 0 || o->group_order > 2) {
+        ag_set_error("group_order must be 0, 1 or 2");
+        return ASSIST_ERROR_N;
+    }
     if (o->warm_start < 0 || o->warm_start > 3 || (o->warm_start && o->group_steps != 2)) {
         ag_set_error("warm_start is 0, 1, 2 or 3; the learned warm start runs in the block-cooperative kernel "
                      "(group_steps = 2)");
@@ -1384,8 +1391,8 @@ extern "C" int assist_gb300_group_plan(int n, const double* t0, const double* t_
                                        const double* params, const float* ratio, int group_order, double gm_sun,
                                        int* order, int* gstart, int* gsize, int* n_groups) {
     if (n < 0 || (n > 0 && (!t0 || !t_end || !state || !order || !gstart || !gsize || !n_groups)) ||
-        (group_order != 0 && group_order != 1) || !(gm_sun > 0.0)) {
-        ag_set_error("group plan: n >= 0, every output array, group_order 0 or 1 and gm_sun > 0 are required");
+        (group_order < 0 || group_order > 2) || !(gm_sun > 0.0)) {
+        ag_set_error("group plan: n >= 0, every output array, group_order 0, 1 or 2 and gm_sun > 0 are required");
         return ASSIST_ERROR_N;
     }
     if (n_groups) *n_groups = 0;

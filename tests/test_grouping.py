@@ -83,6 +83,33 @@ def test_order_inside_a_bucket():
         assert a[0] < b[0] or (a[0] == b[0] and a[1] <= b[1] * (1 + 1e-12) + 1e-9), (i, a, b)
 
 
+def test_order_with_eccentricity_key():
+    """group_order 2: inside a class, length bins, then eccentricity in
+    eighths, then time to pericentre passage."""
+    from assist_gb300 import batch
+    t0, te, st, prm, tp, q = _pop(seed=4)
+    order, groups = batch.group_plan(t0, te, st, params=prm, group_order=2)
+    n = t0.size
+    assert sorted(order.tolist()) == list(range(n)) and sorted(np.concatenate(groups).tolist()) == list(range(n))
+    r = np.linalg.norm(st[:, :3], axis=1); v2 = (st[:, 3:] ** 2).sum(1); rv = (st[:, :3] * st[:, 3:]).sum(1)
+    ecc = np.linalg.norm(((v2 - GM / r)[:, None] * st[:, :3] - rv[:, None] * st[:, 3:]) / GM, axis=1)
+    L = np.abs(te - t0)
+    lbin = -np.floor(16 * np.log2(np.maximum(L, 1e-3)))
+    ebin = np.floor(8 * np.clip(ecc, 0, 0.999))
+    bucket = np.floor(8 * np.log2(q ** 1.5))
+    cls = np.stack([t0, (te < t0).astype(float), (prm[:, 0] != 0).astype(float), bucket], axis=1)
+    o = order
+    same = np.all(cls[o[1:]] == cls[o[:-1]], axis=1)
+    k = np.stack([lbin[o], ebin[o], tp[o]], axis=1)
+    bad = 0
+    for i in np.nonzero(same)[0]:
+        a, b = k[i], k[i + 1]
+        ok = (a[0] < b[0]) or (a[0] == b[0] and (a[1] < b[1] or (a[1] == b[1] and a[2] <= b[2] * (1 + 1e-12) + 1e-9)))
+        bad += not ok
+    # an eccentricity within a rounding of an eighth can land in either bin
+    assert bad <= 2, bad
+
+
 def _q(st):
     r = np.linalg.norm(st[:, :3], axis=1); v2 = (st[:, 3:] ** 2).sum(1); rv = (st[:, :3] * st[:, 3:]).sum(1)
     ev = ((v2 - GM / r)[:, None] * st[:, :3] - rv[:, None] * st[:, 3:]) / GM

@@ -502,11 +502,13 @@ extern "C" void assist_integrate_or_interpolate(struct assist_extras* ax, double
     } else if (sim->ri_ias15.br.p0 == nullptr) {
         std::printf("Error: cannot interpolate before first timestep is complete (h=%e).\n", h);
     } else {
-        double* b[7] = {sim->ri_ias15.br.p0, sim->ri_ias15.br.p1, sim->ri_ias15.br.p2, sim->ri_ias15.br.p3,
-                        sim->ri_ias15.br.p4, sim->ri_ias15.br.p5, sim->ri_ias15.br.p6};
+        /* the polynomial of the last step, evaluated on the device from the
+         * step-start state and b it holds */
         std::memcpy(ax->current_state, sim->particles, sizeof(struct reb_particle) * (size_t)N);
-        gauss_radau_eval(sim->ri_ias15.x0, sim->ri_ias15.v0, sim->ri_ias15.a0, b, sim->dt_last_done, h, N,
-                         ax->current_state);
+        if (ag_shared_interpolate(workspace(ax), N, sim->dt_last_done, h, ax->current_state)) {
+            reb_simulation_error(sim, ("(ASSIST gb300) device interpolation failed: " + g_last_error).c_str());
+            sim->status = REB_STATUS_GENERIC_ERROR;
+        }
     }
     struct reb_particle* p = sim->particles;
     sim->particles = ax->current_state;

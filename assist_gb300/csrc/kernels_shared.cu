@@ -532,6 +532,59 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     return 0;
 }
 
+/* State at fraction h of the last accepted step of size dt, from that step's
+ * start (x, v, a) and converged b, as ASSIST interpolates it
+ * (src/assist.c:556-597: the same s- and sv-coefficient recurrences and the
+ * same sums, without contraction), into XP, VP. */
+__global__ void sh_k_interp(ShView W, int n, double dt, double h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s[9], sv[8];
+    s[0] = __dmul_rn(dt, h);
+    s[1] = __ddiv_rn(__dmul_rn(s[0], s[0]), 2.);
+    s[2] = __ddiv_rn(__dmul_rn(s[1], h), 3.);
+    s[3] = __ddiv_rn(__dmul_rn(s[2], h), 2.);
+    s[4] = __ddiv_rn(__dmul_rn(__dmul_rn(3., s[3]), h), 5.);
+    s[5] = __ddiv_rn(__dmul_rn(__dmul_rn(2., s[4]), h), 3.);
+    s[6] = __ddiv_rn(__dmul_rn(__dmul_rn(5., s[5]), h), 7.);
+    s[7] = __ddiv_rn(__dmul_rn(__dmul_rn(3., s[6]), h), 4.);
+    s[8] = __ddiv_rn(__dmul_rn(__dmul_rn(7., s[7]), h), 9.);
+    sv[0] = __dmul_rn(dt, h);
+    for (int k = 1; k < 8; k++) sv[k] = __ddiv_rn(__dmul_rn(__dmul_rn((double)k, sv[k - 1]), h), (double)(k + 1));
+    for (int k = 0; k < 3; k++) {
+        double x = __dmul_rn(s[8], W(S_BR + 6, k, i));
+        for (int q = 5; q >= 0; q--) x = __dadd_rn(x, __dmul_rn(s[q + 2], W(S_BR + q, k, i)));
+        x = __dadd_rn(x, __dmul_rn(s[1], W(S_PA, k, i)));
+        x = __dadd_rn(x, __dmul_rn(s[0], W(S_PV, k, i)));
+        double v = __dmul_rn(sv[7], W(S_BR + 6, k, i));
+        for (int q = 5; q >= 0; q--) v = __dadd_rn(v, __dmul_rn(sv[q + 1], W(S_BR + q, k, i)));
+        v = __dadd_rn(v, __dmul_rn(sv[0], W(S_PA, k, i)));
+        W(S_XP, k, i) = __dadd_rn(W(S_PX, k, i), x);
+        W(S_VP, k, i) = __dadd_rn(W(S_PV, k, i), v);
+    }
+}
+
+/* Dense output of the drop-in on the device: the n particles at fraction h
+ * of the last step (of size dt) written into out[].x..vz.  Returns 0, or 1
+ * when the device holds no step of these n particles. */
+int ag_shared_interpolate(AgSharedSim* s, int n, double dt, double h, struct reb_particle* out) {
+    if (!s || !s->state_on_device || s->n != n || !s->d_ws) return 1;
+    ShView W{s->d_ws, s->cap};
+    const size_t F = 3 * (size_t)s->cap;
+    sh_k_interp<<<(n + 127) / 128, 128, 0, s->stream>>>(W, n, dt, h);
+    double* hb = s->h_pin;
+    if (ag_cuda_check(cudaGetLastError(), "interpolation kernel") ||
+        ag_cuda_check(cudaMemcpyAsync(hb, W.w + (size_t)S_XP * F, sizeof(double) * 2 * F, cudaMemcpyDeviceToHost,
+                                      s->stream), "interpolation copy") ||
+        ag_cuda_check(cudaStreamSynchronize(s->stream), "interpolation"))
+        return 1;
+    for (int i = 0; i < n; i++) {
+        out[i].x = hb[i]; out[i].y = hb[(size_t)s->cap + i]; out[i].z = hb[2 * (size_t)s->cap + i];
+        out[i].vx = hb[F + i]; out[i].vy = hb[F + (size_t)s->cap + i]; out[i].vz = hb[F + 2 * (size_t)s->cap + i];
+    }
+    return 0;
+}
+
 /* Copy of the shared-step IAS15 tables (diagnostics). out: h[8], rrinv[64], c[49], d[49], fx[72], fv[64]. */
 extern "C" int ag_debug_shared_tables(double* out) {
     int e = sh_tables_init();

@@ -23,5 +23,7 @@ int ag_shared_forces(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, struc
                      const double* params, int* status_out);
 int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, struct reb_simulation* r,
                         const double* params, double tmax, ShIntegrateOut* out);
+/* the n particles at fraction h of the last step (size dt) on the device, into out[] (0, or 1: no such step) */
+int ag_shared_interpolate(AgSharedSim* s, int n, double dt, double h, struct reb_particle* out);
 
 #endif

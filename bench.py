@@ -314,7 +314,8 @@ def ias15_summary(acc, steps):
     return {"kernel_ms_per_step": acc["kernel_ms"] / steps,
             "steps_accepted": acc["steps_accepted"] // steps, "steps_rejected": acc["steps_rejected"] // steps,
             "force_evals": acc["force_evals"] // steps, "body_tables": acc["tables_built"] // steps,
-            "iterations_per_step": acc["pc_iterations"] / max(acc["steps_accepted"] + acc["steps_rejected"], 1)}
+            "iterations_per_step": acc["pc_iterations"] / max(acc["steps_accepted"] + acc["steps_rejected"], 1),
+            "warm_start_used": acc["warm_start_used"] // steps, "warm_start_fallback": acc["warm_start_fallback"] // steps}
 
 
 def extra_config(name, desc, batch, eph, o_cpu, pop, opts, steps, warmup, stream, flush, dev, sample, threads,
@@ -354,6 +355,8 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the extra configuration lines")
     ap.add_argument("--blocks-per-sm", type=int, default=0,
                     help="block-cooperative kernel residency: 0 automatic (the library's choice), 2 or 3")
+    ap.add_argument("--ephem-staging", type=int, default=0,
+                    help="block-cooperative kernel: 0 automatic, 1 .440 record staged in shared memory, 2 not")
     ap.add_argument("--particles", type=int, default=None, help="override the batch size (profiling only)")
     ap.add_argument("--cpu-budget-s", type=float, default=60.0,
                     help="time budget of the oracle's CPU baseline / parity pass over the population")
@@ -384,7 +387,8 @@ def main():
     prm = torch.tensor(pop.params, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
-    opts = batch.options(group_steps=2, warm_start=0, blocks_per_sm=args.blocks_per_sm)
+    opts = batch.options(group_steps=2, warm_start=0, blocks_per_sm=args.blocks_per_sm,
+                         ephem_staging=args.ephem_staging)
     warm_opts = batch.options(group_steps=2, warm_start=1)
     warm_info = None
     if not args.no_warm:
@@ -410,7 +414,8 @@ def main():
     # default kernel's builds on this batch and records the fastest, which
     # the automatic mode then uses; with the learned warm start requested it
     # also times the learned build against them
-    tune = batch.autotune_device(eph, t0, te, st0, params=prm, opts=opts) if args.blocks_per_sm == 0 else None
+    tune = (batch.autotune_device(eph, t0, te, st0, params=prm, opts=opts)
+            if args.blocks_per_sm == 0 and args.ephem_staging == 0 else None)
     tune_warm = None
     if not args.no_warm:
         tune_warm = batch.autotune_device(eph, t0, te, st0, params=prm, opts=warm_opts)
@@ -540,11 +545,14 @@ def main():
         p4 = synth.population(system, "mix", 1 << 20, seed=SEED_POP + 4, t0=T0, log_len=(30.0, 1826.25),
                               nongrav_frac=0.1, close_frac=0.01)
         v4 = np.tile(np.eye(6)[None], (p4.t0.size, 1, 1))
+        w4 = 0 if args.no_warm else 1
         configs.append(extra_config(
             "variational-1048576x6-mixture-5yr", "1,048,576 particles of the mixture, each with 6 first-order "
             "variational particles (unit deviations), lengths logU[30 d, 5 yr], 10% non-gravitational, 1% on close "
-            "Earth approaches (q_min logU[1e-4, 1e-2] AU); plain predictor; value counts real particle-days",
-            batch, eph, o_cpu, p4, batch.options(group_steps=2), 1, 1, stream, flush, dev, 512, threads, var=v4))
+            "Earth approaches (q_min logU[1e-4, 1e-2] AU); %s; value counts real particle-days"
+            % ("learned warm start with the plain-predictor fallbacks" if w4 else "plain predictor"),
+            batch, eph, o_cpu, p4, batch.options(group_steps=2, warm_start=w4), 1, 1, stream, flush, dev, 512,
+            threads, var=v4))
         del p4, v4
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",

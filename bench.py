@@ -357,6 +357,7 @@ def main():
                     help="block-cooperative kernel residency: 0 automatic (the library's choice), 2 or 3")
     ap.add_argument("--ephem-staging", type=int, default=0,
                     help="block-cooperative kernel: 0 automatic, 1 .440 record staged in shared memory, 2 not")
+    ap.add_argument("--group-order", type=int, default=0, help="grouping of the batch (options.group_order)")
     ap.add_argument("--particles", type=int, default=None, help="override the batch size (profiling only)")
     ap.add_argument("--cpu-budget-s", type=float, default=60.0,
                     help="time budget of the oracle's CPU baseline / parity pass over the population")
@@ -388,7 +389,7 @@ def main():
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
     stream = torch.cuda.current_stream(dev)
     opts = batch.options(group_steps=2, warm_start=0, blocks_per_sm=args.blocks_per_sm,
-                         ephem_staging=args.ephem_staging)
+                         ephem_staging=args.ephem_staging, group_order=args.group_order)
     warm_opts = batch.options(group_steps=2, warm_start=1)
     warm_info = None
     if not args.no_warm:
@@ -549,8 +550,9 @@ def main():
         configs.append(extra_config(
             "variational-1048576x6-mixture-5yr", "1,048,576 particles of the mixture, each with 6 first-order "
             "variational particles (unit deviations), lengths logU[30 d, 5 yr], 10% non-gravitational, 1% on close "
-            "Earth approaches (q_min logU[1e-4, 1e-2] AU); %s; value counts real particle-days"
-            % ("learned warm start with the plain-predictor fallbacks" if w4 else "plain predictor"),
+            "Earth approaches (q_min logU[1e-4, 1e-2] AU); " +
+            ("learned warm start with the plain-predictor fallbacks" if w4 else "plain predictor") +
+            "; value counts real particle-days",
             batch, eph, o_cpu, p4, batch.options(group_steps=2, warm_start=w4), 1, 1, stream, flush, dev, 512,
             threads, var=v4))
         del p4, v4

@@ -99,7 +99,10 @@ def test_shared_step_4096_neo_variational_ten_years_and_back(ten_year_files):
     g = _states(sim)
     var0 = np.tile(np.eye(6), (n, 1))
     r, rv, info = O.integrate(8000.0, 8030.0, pop.state, var_state=var0, var_tp=var_tp.astype(np.int32))
-    assert info["status"] == 0 and sim.steps_done == info["accepted"]
+    # one shared step for 4,096 particles: its size comes from maxima over
+    # them, whose last bits differ between the device's and the oracle's
+    # summation orders, and the last step before 8030 can come out either way
+    assert info["status"] == 0 and abs(sim.steps_done - info["accepted"]) <= 1
     assert np.abs(g[:n, :3] - r[:, :3]).max() < 1e-9
     rel = np.abs(g[n:] - rv).reshape(n, 6, 6).max(axis=(1, 2)) / np.abs(rv).reshape(n, 6, 6).max(axis=(1, 2))
     assert rel.max() < 1e-7

@@ -57,31 +57,71 @@ struct AgCoopScratch {
     double ast_h[AG_MAX_AST][3];    /* heliocentric asteroid positions (AU) */
 };
 
-/* One component of a .440 column: the position sum in the reference's exact
- * arithmetic, the velocity sum with fused multiply-adds (the table's Sun
- * velocity enters only the relativistic and non-gravitational terms, where
- * its last-bit rounding is below 1e-24 of the acceleration). */
-__device__ __forceinline__ double ag_colcomp_pos_vfma(const DevEphem& E, const double* rec, int col, int comp, double tf,
-                                                      double* vsum) {
+/* The block's body tables are formed with fused multiply-adds and
+ * multiplications by reciprocals: within an ulp or two of the reference's
+ * operations (a 1e-16 relative change of a body position, far below the
+ * 1e-14 acceleration bar; the drop-in callback, the per-evaluation kernels
+ * and the independent-step kernel keep the reference's exact arithmetic).
+ * The tables are rebuilt for every step's eight node times and are a large
+ * share of a step's FP64 work: the exact sums take a multiply and an add per
+ * term and the reference's divisions expand to many FP64 instructions. */
+
+/* One component of a .440 column (km): the position sum and, with VEL, the
+ * velocity sum (km/s). */
+template <bool VEL>
+__device__ __forceinline__ double ag_colcomp_fused(const DevEphem& E, const double* rec, int col, int comp, double tf,
+                                                   double* vsum) {
     const int ncf = E.col_ncf[col], niv = E.col_niv[col];
-    const double tt = __dmul_rn(tf, (double)niv);
+    const double tt = tf * (double)niv;
     double fl;
     const int b = ag_subinterval(tt, niv, &fl);
-    const double t0 = __dsub_rn(__dmul_rn(2.0, __dsub_rn(tt, fl)), 1.0);
-    const double two_t0 = __dmul_rn(2.0, t0);
+    const double t0 = fma(2.0, tt - fl, -1.0);
+    const double two_t0 = 2.0 * t0;
     const double* P = rec + E.col_off[col] + ncf * (3 * b + comp);
-    double u = __dadd_rn(__dmul_rn(1.0, P[0]), 0.0), v = P[1];
-    u = __dadd_rn(u, __dmul_rn(t0, P[1]));
+    double u = fma(t0, P[1], P[0]), v = P[1];
     double T0 = 1.0, T1 = t0, S0 = 0.0, S1 = 1.0;
     for (int p = 2; p < ncf; p++) {
-        const double Tp = __dsub_rn(__dmul_rn(two_t0, T1), T0);
-        const double Sp = fma(two_t0, S1, fma(2.0, T1, -S0));
-        u = __dadd_rn(u, __dmul_rn(Tp, P[p]));
-        v = fma(Sp, P[p], v);
-        T0 = T1; T1 = Tp; S0 = S1; S1 = Sp;
+        const double Tp = fma(two_t0, T1, -T0);
+        u = fma(Tp, P[p], u);
+        if (VEL) {
+            const double Sp = fma(two_t0, S1, fma(2.0, T1, -S0));
+            v = fma(Sp, P[p], v);
+            S0 = S1; S1 = Sp;
+        }
+        T0 = T1; T1 = Tp;
     }
-    *vsum = v * __ddiv_rn(__ddiv_rn((double)(niv * 2), E.pl_inc), 86400.0);
+    if (VEL) *vsum = v * ((double)(niv * 2) / E.pl_inc / 86400.0);
     return u;
+}
+
+/* One component of an asteroid's heliocentric position (AU) from its SPK
+ * record, with the record's precomputed 1/RADIUS and the segment's
+ * 1/INTLEN. */
+__device__ __forceinline__ int ag_astcomp_fused(const DevEphem& E, int m, int comp, double t, double* out) {
+    const double jd = E.jd_ref + t;
+    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    int n = 0;
+    if (E.ast_nseg[m] > 1) {
+        n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);
+        if (n >= E.ast_nseg[m]) n = E.ast_nseg[m] - 1;
+    }
+    const AgSpkSeg sg = E.segs[E.ast_seg0[m] + n];
+    int b = (int)(((E.jd_ref - sg.init_jd) + t) * sg.inv_intlen_days);
+    if (b >= sg.nrec) b = sg.nrec - 1;
+    if (b < 0) b = 0;
+    const AgRecMeta meta = E.rec_meta[sg.meta_off + b];
+    const int P = sg.P;
+    const double* X = E.spk + sg.data_off + (size_t)b * sg.R + 2 + comp * P;
+    const double z = ((E.jd_ref - meta.x) + t) * meta.z;
+    const double two_z = 2.0 * z;
+    double s = P > 1 ? fma(X[1], z, X[0]) : X[0], T0 = 1.0, T1 = z;
+    for (int q = 2; q < P; q++) {
+        const double Tq = fma(two_z, T1, -T0);
+        s = fma(X[q], Tq, s);
+        T0 = T1; T1 = Tq;
+    }
+    *out = s * (1.0 / 149597870.7);
+    return AG_OK;
 }
 
 /* A body table of one substep time and, per body, the origin minus the body's
@@ -215,10 +255,10 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
                 bad = 1;
             } else if (w0) {
                 /* MER..LUN (columns 0..9), component lane % 3 */
-                S.col[lane / 3][lane % 3] = ag_colcomp_exact<false>(E, rec, lane / 3, lane % 3, tf, nullptr);
+                S.col[lane / 3][lane % 3] = ag_colcomp_fused<false>(E, rec, lane / 3, lane % 3, tf, nullptr);
             } else {
                 double vs;
-                S.col[AG_C_SUN][lane] = ag_colcomp_pos_vfma(E, rec, AG_C_SUN, lane, tf, &vs);
+                S.col[AG_C_SUN][lane] = ag_colcomp_fused<true>(E, rec, AG_C_SUN, lane, tf, &vs);
                 S.sun_v[lane] = vs;
             }
         }
@@ -228,7 +268,7 @@ __device__ __forceinline__ int ag_coop_table_pass1(const DevEphem& E, const Forc
         const bool need = (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) != 0;
         for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
             double h = 0.0;
-            if (ag_astcomp_exact(E, task / 3, task % 3, t, &h) != AG_OK && need) bad = 1;
+            if (ag_astcomp_fused(E, task / 3, task % 3, t, &h) != AG_OK && need) bad = 1;
             S.ast_h[task / 3][task % 3] = h;
         }
     }
@@ -248,7 +288,7 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
             for (int q = tid - 64; q < 3 * E.n_ast; q += 64) {
                 const int comp = q % 3;
                 const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
-                const double xa = __dadd_rn(S.ast_h[q / 3][comp], sun);
+                const double xa = S.ast_h[q / 3][comp] + sun;
                 T.ast[q / 3][comp] = xa;
                 if (bary) CT.rel[AG_NPL + q / 3][comp] = 0.0 - xa;
             }
@@ -257,21 +297,21 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
     if (tid < 33) {
         const int b = tid / 3, comp = tid % 3;
         double u;
-        if (b == AG_EAR) u = __dadd_rn(S.col[AG_C_EMB][comp], __dmul_rn(S.col[AG_C_LUN][comp], E.f_earth));
-        else if (b == AG_MOO) u = __dadd_rn(S.col[AG_C_EMB][comp], __dmul_rn(S.col[AG_C_LUN][comp], E.f_moon));
+        if (b == AG_EAR) u = fma(S.col[AG_C_LUN][comp], E.f_earth, S.col[AG_C_EMB][comp]);
+        else if (b == AG_MOO) u = fma(S.col[AG_C_LUN][comp], E.f_moon, S.col[AG_C_EMB][comp]);
         else u = S.col[ag_col_of(b)][comp];
-        const double x = __ddiv_rn(u, E.pl_cau);
+        const double x = u * E.inv_cau;
         if (comp == 0) T.P.x[b] = x; else if (comp == 1) T.P.y[b] = x; else T.P.z[b] = x;
         if (bary) CT.rel[b][comp] = 0.0 - x;
     } else if (tid < 36) {
         const int comp = tid - 33;
-        const double v = __ddiv_rn(S.sun_v[comp], E.cau_per_day);
+        const double v = S.sun_v[comp] * (86400.0 * E.inv_cau);
         if (comp == 0) T.P.vx[AG_SUN] = v; else if (comp == 1) T.P.vy[AG_SUN] = v; else T.P.vz[AG_SUN] = v;
     } else if (tid >= 64) {
         for (int task = tid - 64; task < 3 * E.n_ast; task += 64) {
             const int comp = task % 3;
-            const double sun = __ddiv_rn(S.col[AG_C_SUN][comp], E.pl_cau);
-            const double xa = __dadd_rn(S.ast_h[task / 3][comp], sun);
+            const double sun = S.col[AG_C_SUN][comp] * E.inv_cau;
+            const double xa = S.ast_h[task / 3][comp] + sun;
             T.ast[task / 3][comp] = xa;
             if (bary) CT.rel[AG_NPL + task / 3][comp] = 0.0 - xa;
         }

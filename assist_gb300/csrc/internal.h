@@ -10,6 +10,17 @@
 
 #include "device_ephem.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
+/* A named NVTX range over a host scope (the phases of a batched call show
+ * in a profiler's timeline; without a profiler attached it costs nothing). */
+struct AgRange {
+    explicit AgRange(const char* name) { nvtxRangePushA(name); }
+    ~AgRange() { nvtxRangePop(); }
+    AgRange(const AgRange&) = delete;
+    AgRange& operator=(const AgRange&) = delete;
+};
+
 struct ForceCfg;
 
 /* Particle I/O of the shared-time force kernel (one REBOUND simulation). */

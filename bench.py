@@ -207,8 +207,10 @@ def parity(idx, ref, rstat, gpu, gstat, vref=None, vgpu=None):
     """End-state agreement on the particles idx (both completed)."""
     both = (rstat == 0) & (gstat[idx] == 0)
     d = np.abs(gpu[idx][both, :3] - ref[both, :3]).max(axis=1) if both.any() else np.zeros(1)
+    mism = np.nonzero(rstat != gstat[idx])[0]
     out = {"n": int(both.sum()), "sampled": int(len(idx)), "median_au": float(np.median(d)), "max_au": float(d.max()),
-           "over_1e-9": int((d > 1e-9).sum()), "status_mismatches": int((rstat != gstat[idx]).sum())}
+           "over_1e-9": int((d > 1e-9).sum()), "status_mismatches": int(mism.size),
+           "mismatched_status_gpu_oracle": [[int(gstat[idx][k]), int(rstat[k])] for k in mism[:8]]}
     if vref is not None:
         vg = vgpu[idx][both]
         vr = vref[both]

@@ -221,9 +221,9 @@ struct assist_gb300_options {
                                stops with ASSIST_GB300_STEP_UNDERFLOW (an impact: any orbit
                                outside a body needs steps > 1e-4 day); 0 disables */
     int group_order;        /* how groups are formed (group_steps 1, 2): 0 (default) perihelion
-                               distance, length, then time of pericentre passage; 1 orbit size,
-                               length, then mean anomaly; 2 as 0 with eccentricity in eighths
-                               between length and pericentre time */
+                               distance, length, eccentricity in eighths, then time of pericentre
+                               passage; 1 orbit size, length, then mean anomaly; 2 as 0 without
+                               the eccentricity key */
     int blocks_per_sm;      /* group_steps 2 without variational particles or warm start:
                                0 (default) three resident blocks per SM when the batch has at
                                least 8 groups per such block, else two; 2 or 3 force it */

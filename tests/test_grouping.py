@@ -1,9 +1,9 @@
 """The grouping of the grouped batched kernels (host logic, no GPU): groups
 partition the batch, hold at most 32 particles that share start time,
 direction and the presence of non-gravitational parameters, sit in one
-perihelion bucket, are ordered inside it by length and then by the time of
-pericentre passage, and are queued most expensive first; the encounter ratio
-raises a group's place in the queue."""
+perihelion bucket, are ordered inside it by length, eccentricity and then by
+the time of pericentre passage, and are queued most expensive first; the
+encounter ratio raises a group's place in the queue."""
 import numpy as np
 import pytest
 
@@ -66,11 +66,11 @@ def test_groups_partition_and_share_class():
 
 
 def test_order_inside_a_bucket():
-    """Within one class the order is length (sixteenth octaves, longest
-    first), then time to pericentre passage."""
+    """group_order 2: within one class the order is length (sixteenth
+    octaves, longest first), then time to pericentre passage."""
     from assist_gb300 import batch
     t0, te, st, prm, tp, q = _pop(seed=1)
-    order, groups = batch.group_plan(t0, te, st, params=prm)
+    order, groups = batch.group_plan(t0, te, st, params=prm, group_order=2)
     L = np.abs(te - t0)
     lbin = -np.floor(16 * np.log2(np.maximum(L, 1e-3)))
     bucket = np.floor(8 * np.log2(q ** 1.5))
@@ -84,11 +84,11 @@ def test_order_inside_a_bucket():
 
 
 def test_order_with_eccentricity_key():
-    """group_order 2: inside a class, length bins, then eccentricity in
-    eighths, then time to pericentre passage."""
+    """The default grouping: inside a class, length bins, then eccentricity
+    in eighths, then time to pericentre passage."""
     from assist_gb300 import batch
     t0, te, st, prm, tp, q = _pop(seed=4)
-    order, groups = batch.group_plan(t0, te, st, params=prm, group_order=2)
+    order, groups = batch.group_plan(t0, te, st, params=prm)
     n = t0.size
     assert sorted(order.tolist()) == list(range(n)) and sorted(np.concatenate(groups).tolist()) == list(range(n))
     r = np.linalg.norm(st[:, :3], axis=1); v2 = (st[:, 3:] ** 2).sum(1); rv = (st[:, :3] * st[:, 3:]).sum(1)

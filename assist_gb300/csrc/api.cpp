@@ -1103,9 +1103,11 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         if (ag_cuda_check(cudaMalloc(&g_batch.d_grp, sizeof(int) * 2 * (size_t)ng), "cudaMalloc(groups)")) return ASSIST_ERROR_EPHEM_FILE;
         g_batch.grp_cap = ng;
     }
+    /* counters: 8 words, then the per-SM block counters of the role rotation */
+    const size_t cnt_bytes = 8 * sizeof(unsigned long long) + AG_SM_SLOTS * sizeof(int);
     if (!g_batch.d_queue) {
         if (ag_cuda_check(cudaMalloc(&g_batch.d_queue, sizeof(int)), "cudaMalloc") ||
-            ag_cuda_check(cudaMalloc(&g_batch.d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc"))
+            ag_cuda_check(cudaMalloc(&g_batch.d_counters, cnt_bytes), "cudaMalloc"))
             return ASSIST_ERROR_EPHEM_FILE;
     }
     const size_t wsn = ag_batch_ws_doubles(nslots, n_var);
@@ -1124,12 +1126,13 @@ static int ag_integrate_batch(const struct assist_ephem* e, const struct assist_
         cudaMemcpyAsync(g_batch.d_grp + ng, gsize.data(), sizeof(int) * (size_t)ng, cudaMemcpyHostToDevice, s);
     }
     cudaMemsetAsync(g_batch.d_queue, 0, sizeof(int), s);
-    cudaMemsetAsync(g_batch.d_counters, 0, 8 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(g_batch.d_counters, 0, cnt_bytes, s);
     AgBatchArgs a;
     std::memset(&a, 0, sizeof(a));
     a.n = n; a.nslots = nslots; a.order = g_batch.d_order; a.queue = g_batch.d_queue;
     a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
     a.status = d_status; a.ws = g_batch.d_ws; a.counters = g_batch.d_counters;
+    a.sm_slots = reinterpret_cast<int*>(g_batch.d_counters + 8);
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
     a.dt_floor = o->dt_floor;
     if (grouped) { a.grp_start = g_batch.d_grp; a.grp_size = g_batch.d_grp + ng; a.n_groups = ng; }
@@ -1240,7 +1243,8 @@ extern "C" int assist_gb300_plan_create(const struct assist_ephem* e, const stru
     bool ok = !ag_cuda_check(cudaMalloc(&p->d_order, sizeof(int) * (size_t)n), "cudaMalloc(plan order)") &&
               (!P.grouped || !ag_cuda_check(cudaMalloc(&p->d_grp, sizeof(int) * 2 * (size_t)ng), "cudaMalloc(plan groups)")) &&
               !ag_cuda_check(cudaMalloc(&p->d_queue, sizeof(int)), "cudaMalloc(plan queue)") &&
-              !ag_cuda_check(cudaMalloc(&p->d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc(plan counters)") &&
+              !ag_cuda_check(cudaMalloc(&p->d_counters, 8 * sizeof(unsigned long long) + AG_SM_SLOTS * sizeof(int)),
+                             "cudaMalloc(plan counters)") &&
               !ag_cuda_check(cudaMalloc(&p->d_ws, sizeof(double) * wsn), "cudaMalloc(plan IAS15 slots)") &&
               !ag_cuda_check(cudaMallocHost(&p->h_counters, 8 * sizeof(unsigned long long)), "cudaMallocHost(plan counters)") &&
               !ag_cuda_check(cudaMemcpy(p->d_order, P.order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice), "plan order") &&
@@ -1255,6 +1259,7 @@ extern "C" int assist_gb300_plan_create(const struct assist_ephem* e, const stru
     a.n = n; a.nslots = P.nslots; a.order = p->d_order; a.queue = p->d_queue;
     a.t0 = d_t0; a.t_end = d_t_end; a.state = d_state; a.params = d_params; a.var_state = d_var_state;
     a.status = d_status; a.ws = p->d_ws; a.counters = p->d_counters;
+    a.sm_slots = reinterpret_cast<int*>(p->d_counters + 8);
     a.epsilon = o->epsilon; a.min_dt = o->min_dt; a.dt0 = o->dt0; a.max_steps = o->max_steps;
     a.dt_floor = o->dt_floor;
     if (P.grouped) { a.grp_start = p->d_grp; a.grp_size = p->d_grp + ng; a.n_groups = ng; }
@@ -1273,7 +1278,7 @@ extern "C" int assist_gb300_plan_create(const struct assist_ephem* e, const stru
     ok = !ag_cuda_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "plan capture");
     if (ok) {
         cudaMemsetAsync(p->d_queue, 0, sizeof(int), cs);
-        cudaMemsetAsync(p->d_counters, 0, 8 * sizeof(unsigned long long), cs);
+        cudaMemsetAsync(p->d_counters, 0, 8 * sizeof(unsigned long long) + AG_SM_SLOTS * sizeof(int), cs);
         le = P.coop ? ag_launch_coop(P.D, P.c, a, n_var, P.occ, P.stage, cs)
                     : (P.grouped ? ag_launch_group(P.D, P.c, a, n_var, cs) : ag_launch_batch(P.D, P.c, a, n_var, P.tpb, cs));
         cudaMemcpyAsync(p->h_counters, p->d_counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, cs);

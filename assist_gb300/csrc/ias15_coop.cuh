@@ -593,6 +593,7 @@ struct AgCoopShared {
     int g, stop;
     int stage_fail;                                 /* a staged record copy did not complete */
     int wg_off;                                     /* learned warm start switched off for this group */
+    int rot;                                        /* role rotation of this block */
 };
 
 /* Shared buffers of the learned warm start (dynamic shared memory, present
@@ -710,8 +711,24 @@ template <int NV, bool WARM, int OCC = 2, bool STAGE = false>
 __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict__ Ep, ForceCfg cf, AgBatchArgs A) {
     constexpr int C = 3 * (1 + NV);
     const DevEphem& E = *Ep;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     __shared__ AgCoopShared<NV> S;
+    /* Role rotation: warp w of a block runs on sub-partition w % 4 of its SM,
+     * and the four roles (planets / relativity / asteroids / asteroids and
+     * Sun J2) do unequal FP64 work.  Blocks sharing an SM take successive
+     * rotations (a per-SM counter) so that each sub-partition's FP64 pipe
+     * serves a mix of roles; within a block everything below uses the
+     * logical warp index wid and thread index tid. */
+    if (threadIdx.x == 0) {
+        int r = 0;
+        if (A.sm_slots) {
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            r = atomicAdd(&A.sm_slots[smid & (AG_SM_SLOTS - 1)], 1) & 3;
+        }
+        S.rot = r;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = ((threadIdx.x >> 5) + S.rot) & 3, tid = (wid << 5) | lane;
     AgCoopTab& Tab = S.tab[0];
     const int slot = blockIdx.x * 32 + lane;
     extern __shared__ __align__(16) unsigned char ag_dyn_smem[];

@@ -37,6 +37,8 @@ struct AgForceIO {
     int* status;            /* one int, atomically max-ed with an ASSIST status */
 };
 
+#define AG_SM_SLOTS 1024
+
 /* Device-side state of the batched integrator. */
 struct AgBatchArgs {
     int n;                          /* particles */
@@ -50,7 +52,9 @@ struct AgBatchArgs {
     double* var_state;              /* [n][NV][6] */
     int* status;                    /* [n] or null */
     double* ws;                     /* per-slot workspace, see kernels_ias15.cu */
-    unsigned long long* counters;   /* accepted, rejected, evals, iterations, warm used, warm fallback */
+    unsigned long long* counters;   /* accepted, rejected, evals, iterations, warm used, warm fallback, tables */
+    int* sm_slots;                  /* AG_SM_SLOTS per-SM block counters, zero at launch (block-cooperative
+                                       kernel's role rotation), or null */
     double epsilon, min_dt, dt0, dt_floor;
     long long max_steps;
     long long watchdog_cycles;      /* per-thread clock64 budget; 0 = none */

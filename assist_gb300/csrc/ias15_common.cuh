@@ -111,7 +111,9 @@ __device__ __forceinline__ void ag_predict_next(const Ws<C>& W, double ratio) {
 }
 
 
+#ifndef AG_FULL
 #define AG_FULL 0xffffffffu
+#endif
 
 __device__ __forceinline__ double warp_min(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(AG_FULL, v, o));

@@ -6,12 +6,16 @@
  *
  * All per-particle state stays on the device between steps.  A step is
  * a start evaluation (node 0) and predictor-corrector iterations of 7 node
- * evaluations; each node is predict -> force table kernel -> update.  The
- * update of node 7 also reduces max|delta b6|, max|a| and max|b6| over the
- * real particles (the global error measures of adaptive_mode = 1) into three
- * words the host reads back once per iteration to decide convergence,
- * acceptance and the next step size, with the same rules as the batched
- * kernel (kernels_ias15.cu).
+ * evaluations; each node is predict -> forces -> update, all inside one
+ * kernel (sh_k_step) whose 128-thread blocks each own 32 real particles and
+ * their variational particles and build the step's eight body tables once.
+ * The update of node 7 also reduces max|delta b6|, max|a| and max|b6| over
+ * the real particles (the global error measures of adaptive_mode = 1).  With
+ * several blocks a launch is one iteration and the host reads the three
+ * maxima back to decide convergence; with one block (up to 32 real
+ * particles) a launch is the whole predictor-corrector loop of the step.  The
+ * host then decides acceptance and the next step size, with the same rules as
+ * the batched kernel (kernels_ias15.cu).
  */
 #include <cuda_runtime.h>
 #include <cmath>
@@ -22,6 +26,8 @@
 #include "ias15_constants.h"
 #include "internal.h"
 #include "shared_sim.h"
+#include "table_forces.cuh"
+#include "coop_forces.cuh"
 
 __constant__ double sh_h[8];
 __constant__ double sh_rrinv[8][8];
@@ -71,11 +77,12 @@ struct ShView {
     __device__ __forceinline__ double& operator()(int f, int k, int i) const { return w[((size_t)f * 3 + k) * stride + i]; }
 };
 
-__global__ void sh_k_predict(ShView W, int n, int node, double hstep) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+/* Predictor of component k of particle i at node `node` of a step of size
+ * hstep (node 0: the start state). */
+__device__ __forceinline__ void sh_predict(const ShView& W, int i, int k, int node, double hstep) {
     if (node == 0) {
-        for (int k = 0; k < 3; k++) { W(S_XP, k, i) = W(S_X0, k, i); W(S_VP, k, i) = W(S_V0, k, i); }
+        W(S_XP, k, i) = W(S_X0, k, i);
+        W(S_VP, k, i) = W(S_V0, k, i);
         return;
     }
     const double hn = sh_h[node];
@@ -83,76 +90,281 @@ __global__ void sh_k_predict(ShView W, int n, int node, double hstep) {
     sx[0] = hstep * hn;
     sx[1] = sx[0] * sx[0] * 0.5;
 #pragma unroll
-    for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * sh_fx[node][k];
+    for (int q = 2; q < 9; q++) sx[q] = sx[q - 1] * sh_fx[node][q];
     sv[0] = hstep * hn;
 #pragma unroll
-    for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * sh_fv[node][k];
-    for (int k = 0; k < 3; k++) {
-        double px = sx[8] * W(S_B + 6, k, i);
+    for (int q = 1; q < 8; q++) sv[q] = sv[q - 1] * sh_fv[node][q];
+    double px = sx[8] * W(S_B + 6, k, i);
 #pragma unroll
-        for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(S_B + j, k, i), px);
-        px = fma(sx[1], W(S_A0, k, i), px);
-        px = fma(sx[0], W(S_V0, k, i), px);
-        W(S_XP, k, i) = W(S_X0, k, i) + (px + W(S_XC, k, i));
-        double pv = sv[7] * W(S_B + 6, k, i);
+    for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(S_B + j, k, i), px);
+    px = fma(sx[1], W(S_A0, k, i), px);
+    px = fma(sx[0], W(S_V0, k, i), px);
+    W(S_XP, k, i) = W(S_X0, k, i) + (px + W(S_XC, k, i));
+    double pv = sv[7] * W(S_B + 6, k, i);
 #pragma unroll
-        for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(S_B + j, k, i), pv);
-        pv = fma(sv[0], W(S_A0, k, i), pv);
-        W(S_VP, k, i) = W(S_V0, k, i) + (pv + W(S_VC, k, i));
+    for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(S_B + j, k, i), pv);
+    pv = fma(sv[0], W(S_A0, k, i), pv);
+    W(S_VP, k, i) = W(S_V0, k, i) + (pv + W(S_VC, k, i));
+}
+
+/* Start of a step for component k: a0 from the node-0 force, g from the
+ * predicted b. */
+__device__ __forceinline__ void sh_start(const ShView& W, int i, int k) {
+    W(S_A0, k, i) = W(S_AT, k, i);
+    double b[7];
+#pragma unroll
+    for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        double s = b[j];
+#pragma unroll
+        for (int q = j + 1; q < 7; q++) s = fma(b[q], sh_d[j][q], s);
+        W(S_G + j, k, i) = s;
     }
 }
 
-__global__ void sh_k_start(ShView W, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    for (int k = 0; k < 3; k++) {
-        W(S_A0, k, i) = W(S_AT, k, i);
-        double b[7];
-#pragma unroll
-        for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
-#pragma unroll
-        for (int j = 0; j < 7; j++) {
-            double s = b[j];
-#pragma unroll
-            for (int q = j + 1; q < 7; q++) s = fma(b[q], sh_d[j][q], s);
-            W(S_G + j, k, i) = s;
-        }
+/* Corrector of component k of particle i at node `node`: g and b from the
+ * node's force.  At node 7 the real particles' |delta b6|, |a| and |b6| enter
+ * the running maxima (normal values only, as REBOUND's isnormal tests). */
+__device__ __forceinline__ void sh_update(const ShView& W, int i, int k, int n_real, int node, double& mdb, double& ma,
+                                          double& mb) {
+    const double at = W(S_AT, k, i);
+    double gn = (at - W(S_A0, k, i)) * sh_rrinv[node][0];
+    for (int j = 1; j < node; j++) gn = (gn - W(S_G + j - 1, k, i)) * sh_rrinv[node][j];
+    const double delta = gn - W(S_G + node - 1, k, i);
+    W(S_G + node - 1, k, i) = gn;
+    for (int q = 0; q < node - 1; q++) W(S_B + q, k, i) = fma(delta, sh_c[node - 1][q], W(S_B + q, k, i));
+    W(S_B + node - 1, k, i) += delta;
+    if (node == 7 && i < n_real) {
+        const double aa = fabs(at), db = fabs(delta), bb = fabs(W(S_B + 6, k, i));
+        if (ag_isnormal_pos(aa) && aa > ma) ma = aa;
+        if (ag_isnormal_pos(db) && db > mdb) mdb = db;
+        if (ag_isnormal_pos(bb) && bb > mb) mb = bb;
     }
 }
 
-/* Reductions into red[0..2] (bit patterns of non-negative doubles compare
- * like unsigned integers): max|delta b6|, max|a|, max|b6| over real particles. */
-__global__ void sh_k_update(ShView W, int n, int n_real, int node, unsigned long long* red) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double mdb = 0.0, ma = 0.0, mb = 0.0;
-    if (i < n) {
-        for (int k = 0; k < 3; k++) {
-            const double at = W(S_AT, k, i);
-            double gn = (at - W(S_A0, k, i)) * sh_rrinv[node][0];
-            for (int j = 1; j < node; j++) gn = (gn - W(S_G + j - 1, k, i)) * sh_rrinv[node][j];
-            const double delta = gn - W(S_G + node - 1, k, i);
-            W(S_G + node - 1, k, i) = gn;
-            for (int q = 0; q < node - 1; q++) W(S_B + q, k, i) = fma(delta, sh_c[node - 1][q], W(S_B + q, k, i));
-            W(S_B + node - 1, k, i) += delta;
-            if (node == 7 && i < n_real) {
-                const double aa = fabs(at), db = fabs(delta), bb = fabs(W(S_B + 6, k, i));
-                if (ag_isnormal_pos(aa) && aa > ma) ma = aa;
-                if (ag_isnormal_pos(db) && db > mdb) mdb = db;
-                if (ag_isnormal_pos(bb) && bb > mb) mb = bb;
+/* ------------------------------------------------------------------ step kernel
+ *
+ * One launch does the predictor-corrector work of a step for a block of 32
+ * real particles (lane l of every warp: real particle 32 b + l) and their
+ * variational particles, with the block-cooperative force evaluation of the
+ * batched kernel: the four warps split each particle's force terms (their
+ * partial sums added ((w3 + w2) + w1) + w0), and the eight node tables of the
+ * step are built once, at its start, by the whole block (the node times do
+ * not change while the corrector iterates).  A variational particle's
+ * acceleration is its real particle's Jacobian (summed from the warps'
+ * partial Jacobians) applied to its state.  The IAS15 state stays in global
+ * memory; its predictor and corrector run as one task per particle component
+ * over the block's threads.  Block b predicts and corrects the particles of
+ * plist[pstart[b] .. pstart[b+1]): its real particles, their variational
+ * particles and (last block) any particle no real particle lists, so that a
+ * node needs no grid-wide barrier.  The maxima over the real particles
+ * (max|delta b6|, max|a|, max|b6|; bit patterns of non-negative doubles
+ * order like unsigned integers) go to red[0..2].
+ *
+ * Several blocks: one iteration per launch and the host decides convergence;
+ * the first launch of a step (`first`: node 0 and the tables) leaves the
+ * tables in gtab for the launches after it.  One block (up to 32 real
+ * particles): every iteration of the step in one launch, with the host's
+ * convergence rule (relative corrector change below 1e-16, no longer
+ * decreasing after two iterations, or 12 iterations) and the iteration count
+ * in red[3].  A node time outside the ephemeris sets ASSIST's coverage status
+ * and ends the launch. */
+struct ShStepArgs {
+    ShView W;
+    AgForceIO io;            /* x, v, a: the predicted states and accelerations */
+    const int* vowner;       /* real particle of each variational entry of io */
+    const int* plist;
+    const int* pstart;
+    unsigned long long* red;
+    AgCoopTab* gtab;         /* the step's eight node tables (several blocks) */
+    double tn[8];            /* node times: t + (tc + hstep h_n), from the host */
+    double hstep;
+    int first;
+};
+
+struct ShStepSmem {
+    AgCoopTab tab[8];
+    AgCoopScratch scr;
+    AgCoopSeps seps;
+    double pa[4][3][32];     /* partial accelerations of the four warps */
+    double pj[4][18][32];    /* partial Jacobians; pj[0] holds their sum */
+    double pja[9][32];       /* d acc / dA of the non-gravitational term (warp 0) */
+    int png[32];
+    unsigned long long red[3];
+    int more;
+};
+
+/* Accelerations of the block's particles at node n (table S.tab[n]) into
+ * io.a; ends with a block barrier. */
+__device__ __forceinline__ void sh_step_forces(ShStepSmem& S, const ShStepArgs& A, const DevEphem& E, const ForceCfg& c,
+                                               int n, bool jac, int v0, int v1) {
+    const AgForceIO& io = A.io;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, r0 = 32 * blockIdx.x;
+    const int ir = r0 + lane;
+    const bool live = ir < io.n_real;
+    const AgCoopTab& T = S.tab[n];
+    double xp[3] = {0.0, 0.0, 0.0}, vp[3] = {0.0, 0.0, 0.0}, prm[3] = {0.0, 0.0, 0.0};
+    const double* Ap = nullptr;
+    if (live) {
+        for (int k = 0; k < 3; k++) { xp[k] = io.x[k * io.stride + ir]; vp[k] = io.v[k * io.stride + ir]; }
+        if (io.params) { prm[0] = io.params[3 * ir]; prm[1] = io.params[3 * ir + 1]; prm[2] = io.params[3 * ir + 2]; Ap = prm; }
+    }
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (jac) {
+        if (live) {
+            double J[3][6], JA[3][3];
+            bool ng = false;
+            if (wid == 0) ag_coop_force_part<true>(0, T, E, c, xp, vp, Ap, acc, J, JA, &ng);
+            else ag_coop_force_part<true>(wid, T, E, c, xp, vp, Ap, acc, J);
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 6; b++) S.pj[wid][6 * a + b][lane] = J[a][b];
+            if (wid == 0) {
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) S.pja[3 * a + b][lane] = JA[a][b];
+                S.png[lane] = ng;
             }
         }
+    } else if (wid < 2) {
+        ag_coop_force_split01(wid, live, S.seps, lane, T, E, c, xp, vp, Ap, acc);
+    } else if (live) {
+        ag_coop_force_part<false>(wid, T, E, c, xp, vp, Ap, acc, nullptr);
     }
-    if (node != 7) return;
-    for (int o = 16; o > 0; o >>= 1) {
-        mdb = fmax(mdb, __shfl_xor_sync(0xffffffffu, mdb, o));
-        ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
-        mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    if (live) { S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2]; }
+    __syncthreads();
+    if (tid < 96 && r0 + lane < io.n_real) {
+        const int k = wid;                       /* component k on warp k */
+        io.a[k * io.stride + ir] = ((S.pa[3][k][lane] + S.pa[2][k][lane]) + S.pa[1][k][lane]) + S.pa[0][k][lane];
+        if (jac)
+            for (int b = 0; b < 6; b++) {
+                const int e = 6 * k + b;
+                S.pj[0][e][lane] = ((S.pj[3][e][lane] + S.pj[2][e][lane]) + S.pj[1][e][lane]) + S.pj[0][e][lane];
+            }
     }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&red[0], (unsigned long long)__double_as_longlong(mdb));
-        atomicMax(&red[1], (unsigned long long)__double_as_longlong(ma));
-        atomicMax(&red[2], (unsigned long long)__double_as_longlong(mb));
+    if (jac) {
+        __syncthreads();
+        for (int q = v0 + tid; q < v1; q += blockDim.x) {
+            const int p = io.var_index[q], l = A.vowner[q] - r0;
+            const int cfg = io.var_cfg ? io.var_cfg[q] : -1;
+            double J[3][6], JA[3][3];
+            for (int a = 0; a < 3; a++) {
+                for (int b = 0; b < 6; b++) J[a][b] = S.pj[0][6 * a + b][l];
+                for (int b = 0; b < 3; b++) JA[a][b] = S.pja[3 * a + b][l];
+            }
+            const double dx[3] = {io.x[p], io.x[io.stride + p], io.x[2 * io.stride + p]};
+            const double dv[3] = {io.v[p], io.v[io.stride + p], io.v[2 * io.stride + p]};
+            double dA[3] = {0.0, 0.0, 0.0};
+            if (io.params && cfg >= 0) {
+                const size_t r = 3 * (size_t)(io.n_real + cfg);
+                dA[0] = io.params[r]; dA[1] = io.params[r + 1]; dA[2] = io.params[r + 2];
+            }
+            double out[3];
+            ag_apply_jac(J, JA, S.png[l] != 0, dx, dv, dA, out);
+            io.a[p] = out[0]; io.a[io.stride + p] = out[1]; io.a[2 * io.stride + p] = out[2];
+        }
     }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep, ForceCfg c, ShStepArgs A) {
+    extern __shared__ __align__(16) unsigned char sh_smem[];
+    ShStepSmem& S = *reinterpret_cast<ShStepSmem*>(sh_smem);
+    const DevEphem& E = *Ep;
+    const ShView& W = A.W;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nt = blockDim.x;
+    const int q0 = 3 * A.pstart[blockIdx.x], q1 = 3 * A.pstart[blockIdx.x + 1];   /* (particle, component) tasks */
+    const int n_real = A.io.n_real, r0 = 32 * blockIdx.x, r1 = min(r0 + 32, n_real);
+    const int v0 = (A.io.var_start && r0 < r1) ? A.io.var_start[r0] : 0;
+    const int v1 = (A.io.var_start && r0 < r1) ? A.io.var_start[r1] : 0;
+    const bool jac = v1 > v0;                    /* block-uniform */
+    const bool single = gridDim.x == 1;
+    if (A.first) {
+        /* the step's eight node tables */
+        int bad = 0;
+        for (int n = 0; n < 8; n++) {
+            AgStageCursor cur;
+            int stage_fail = 0;
+            bad |= ag_coop_table_pass1<false>(E, c, A.tn[n], S.scr, S.tab[n], tid, nullptr, cur, &stage_fail);
+            __syncthreads();
+            ag_coop_table_pass2(E, c, A.tn[n], S.tab[n], S.scr, tid);
+            __syncthreads();
+            if (c.geocentric == 1) { ag_coop_rel_geo(E, S.tab[n], tid); __syncthreads(); }
+        }
+        if (c.forces & AG_F_EIH)
+            for (int n = wid; n < 8; n += 4) ag_coop_eih_sources(E, c, S.tab[n].T, lane);
+        bad = __syncthreads_or(bad);
+        if (bad) {
+            if (tid == 0) {
+                if (n_real > 0) atomicMax(A.io.status, (int)AG_ERR_COVERAGE);
+                if (single) { A.red[0] = A.red[1] = A.red[2] = 0ull; A.red[3] = 1ull; }
+            }
+            return;
+        }
+        if (!single && blockIdx.x == 0) {
+            const double* src = reinterpret_cast<const double*>(S.tab);
+            double* dst = reinterpret_cast<double*>(A.gtab);
+            for (int q = tid; q < (int)(sizeof(S.tab) / sizeof(double)); q += nt) dst[q] = src[q];
+        }
+        /* node 0: the start of the step */
+        for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, 0, A.hstep);
+        __syncthreads();
+        sh_step_forces(S, A, E, c, 0, jac, v0, v1);
+        for (int q = q0 + tid; q < q1; q += nt) sh_start(W, A.plist[q / 3], q % 3);
+    } else {
+        const double* src = reinterpret_cast<const double*>(A.gtab);
+        double* dst = reinterpret_cast<double*>(S.tab);
+        for (int q = tid; q < (int)(sizeof(S.tab) / sizeof(double)); q += nt) dst[q] = src[q];
+    }
+    double pc_last = 1e300;
+    int iters = 1;
+    while (true) {
+        if (tid < 3) S.red[tid] = 0ull;
+        double mdb = 0.0, ma = 0.0, mb = 0.0;
+        for (int node = 1; node < 8; node++) {
+            for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, node, A.hstep);
+            __syncthreads();
+            sh_step_forces(S, A, E, c, node, jac, v0, v1);
+            for (int q = q0 + tid; q < q1; q += nt) sh_update(W, A.plist[q / 3], q % 3, n_real, node, mdb, ma, mb);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mdb = fmax(mdb, __shfl_xor_sync(0xffffffffu, mdb, o));
+            ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+            mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+        }
+        if (lane == 0) {
+            atomicMax(&S.red[0], (unsigned long long)__double_as_longlong(mdb));
+            atomicMax(&S.red[1], (unsigned long long)__double_as_longlong(ma));
+            atomicMax(&S.red[2], (unsigned long long)__double_as_longlong(mb));
+        }
+        __syncthreads();
+        if (!single) {
+            if (tid < 3) atomicMax(&A.red[tid], S.red[tid]);
+            return;
+        }
+        if (tid == 0) {
+            const double pc_err = __longlong_as_double((long long)S.red[0]) / __longlong_as_double((long long)S.red[1]);
+            const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+            S.more = !conv;
+            pc_last = pc_err;
+            if (conv) {
+                A.red[0] = S.red[0]; A.red[1] = S.red[1]; A.red[2] = S.red[2];
+                A.red[3] = (unsigned long long)iters;
+            }
+        }
+        __syncthreads();
+        if (!S.more) return;
+        iters++;
+    }
+}
+
+static int sh_step_attr(void) {
+    static bool done[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && done[dev]) return 0;
+    const cudaError_t e = cudaFuncSetAttribute(sh_k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ShStepSmem));
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return (int)e;
 }
 
 __device__ __forceinline__ void sh_predict_next(const ShView& W, int i, double ratio) {
@@ -238,6 +450,12 @@ struct AgSharedSim {
     int* d_vindex = nullptr;
     int* d_vcfg = nullptr;
     size_t vcap = 0;
+    int* d_plist = nullptr;       /* particles per block of the step kernel */
+    int* d_pstart = nullptr;
+    int* d_vowner = nullptr;      /* real particle of each variational entry */
+    size_t pcap = 0;
+    int nblocks = 1;
+    AgCoopTab* d_tab = nullptr;   /* the step's node tables (several blocks) */
     unsigned long long* d_red = nullptr;
     int* d_status = nullptr;
     cudaStream_t stream = nullptr;
@@ -255,6 +473,10 @@ void ag_shared_free(AgSharedSim* s) {
     if (s->d_vstart) cudaFree(s->d_vstart);
     if (s->d_vindex) cudaFree(s->d_vindex);
     if (s->d_vcfg) cudaFree(s->d_vcfg);
+    if (s->d_plist) cudaFree(s->d_plist);
+    if (s->d_pstart) cudaFree(s->d_pstart);
+    if (s->d_vowner) cudaFree(s->d_vowner);
+    if (s->d_tab) cudaFree(s->d_tab);
     if (s->d_red) cudaFree(s->d_red);
     if (s->d_status) cudaFree(s->d_status);
     if (s->h_pin) cudaFreeHost(s->h_pin);
@@ -267,6 +489,7 @@ static int sh_reserve(AgSharedSim* s, int n) {
     if (!s->d_red) {
         if (ag_cuda_check(cudaMalloc(&s->d_red, 4 * sizeof(unsigned long long)), "cudaMalloc(red)")) return 1;
         if (ag_cuda_check(cudaMalloc(&s->d_status, sizeof(int)), "cudaMalloc(status)")) return 1;
+        if (ag_cuda_check(cudaMalloc(&s->d_tab, 8 * sizeof(AgCoopTab)), "cudaMalloc(node tables)")) return 1;
     }
     if (n <= s->cap) return 0;
     int cap = n < 64 ? 64 : n;
@@ -319,6 +542,41 @@ static int sh_upload_vars(AgSharedSim* s, struct reb_simulation* r, const double
         cudaMemcpyAsync(s->d_vindex, idx.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s->stream);
         cudaMemcpyAsync(s->d_vcfg, cfg.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s->stream);
     }
+    /* block lists of the step kernel: block b owns real particles
+     * [32 b, 32 b + 32) and their variational particles; particles no real
+     * particle lists go to the last block */
+    const int nb = n_real > 0 ? (n_real + 31) / 32 : 1;
+    std::vector<int> owner((size_t)n, -1), pstart((size_t)nb + 1, 0), plist((size_t)n), vowner(nv + 1, 0);
+    for (int j = 0; j < n_real; j++) owner[(size_t)j] = j / 32;
+    for (int j = 0; j < n_real; j++)
+        for (int q = start[(size_t)j]; q < start[(size_t)j + 1]; q++) {
+            vowner[(size_t)q] = j;
+            if (idx[(size_t)q] >= n_real && owner[(size_t)idx[(size_t)q]] < 0) owner[(size_t)idx[(size_t)q]] = j / 32;
+        }
+    for (int p = 0; p < n; p++) {
+        if (owner[(size_t)p] < 0) owner[(size_t)p] = nb - 1;
+        pstart[(size_t)owner[(size_t)p] + 1]++;
+    }
+    for (int b = 0; b < nb; b++) pstart[(size_t)b + 1] += pstart[(size_t)b];
+    {
+        std::vector<int> at(pstart.begin(), pstart.end() - 1);
+        for (int p = 0; p < n; p++) plist[(size_t)at[(size_t)owner[(size_t)p]]++] = p;
+    }
+    if ((size_t)n + nb + nv + 1 > s->pcap) {
+        if (s->d_plist) cudaFree(s->d_plist);
+        if (s->d_pstart) cudaFree(s->d_pstart);
+        if (s->d_vowner) cudaFree(s->d_vowner);
+        s->d_plist = s->d_pstart = s->d_vowner = nullptr;
+        s->pcap = (size_t)n + nb + nv + 1 + 64;
+        if (ag_cuda_check(cudaMalloc(&s->d_plist, sizeof(int) * s->pcap), "cudaMalloc(block lists)") ||
+            ag_cuda_check(cudaMalloc(&s->d_pstart, sizeof(int) * s->pcap), "cudaMalloc(block lists)") ||
+            ag_cuda_check(cudaMalloc(&s->d_vowner, sizeof(int) * s->pcap), "cudaMalloc(block lists)"))
+            return 1;
+    }
+    cudaMemcpyAsync(s->d_plist, plist.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->d_pstart, pstart.data(), sizeof(int) * ((size_t)nb + 1), cudaMemcpyHostToDevice, s->stream);
+    if (nv) cudaMemcpyAsync(s->d_vowner, vowner.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s->stream);
+    s->nblocks = nb;
     io->var_start = nv ? s->d_vstart : nullptr;
     io->var_index = s->d_vindex;
     io->var_cfg = s->d_vcfg;
@@ -385,13 +643,14 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     out->status = 0;
     if (n <= 0 || r->t == tmax) return 0;
     if (sh_tables_init()) return ag_cuda_check(cudaErrorInvalidValue, "IAS15 tables");
+    if (ag_cuda_check((cudaError_t)sh_step_attr(), "IAS15 step kernel shared memory")) return 1;
     if (sh_reserve(s, n)) return 1;
     AgForceIO io;
     std::memset(&io, 0, sizeof(io));
     if (sh_upload_vars(s, r, params, &io)) return 1;
     ShView W{s->d_ws, s->cap};
     const size_t F = 3 * (size_t)s->cap;
-    const int tpb = 128, blocks = (n + tpb - 1) / tpb;
+    const int tpb = 128, blocks = (n + tpb - 1) / tpb, nb = s->nblocks;
     cudaStream_t st = s->stream;
     double dir = tmax >= r->t ? 1.0 : -1.0;
     /* the host particles are authoritative: upload them every call; keep the
@@ -424,7 +683,7 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     double dt = r->dt;
     if (dt * dir <= 0) dt = dir * std::fabs(dt != 0 ? dt : 0.001);
     const double eps = r->ri_ias15.epsilon, min_dt = r->ri_ias15.min_dt;
-    unsigned long long red[3];
+    unsigned long long red[4];
     int hstat = 0;
     long long steps = 0;
     while (s->t != tmax) {
@@ -432,34 +691,47 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
         bool last = false;
         double hstep = dt;
         if (std::fabs(dt) >= std::fabs(rem)) { hstep = rem; last = true; }
-        /* node 0 */
+        ShStepArgs A;
+        A.W = W; A.io = io; A.vowner = s->d_vowner; A.plist = s->d_plist; A.pstart = s->d_pstart; A.red = s->d_red;
+        A.gtab = s->d_tab;
+        A.hstep = hstep;
+        A.tn[0] = s->t;
+        for (int node = 1; node < 8; node++) A.tn[node] = s->t + (s->tc + hstep * h_nodes[node]);
+        A.first = 1;
         cudaMemsetAsync(s->d_status, 0, sizeof(int), st);
-        sh_k_predict<<<blocks, tpb, 0, st>>>(W, n, 0, hstep);
-        ag_launch_forces_table(E, c, s->t, io, st);
-        sh_k_start<<<blocks, tpb, 0, st>>>(W, n);
-        out->evals++;
-        double pc_last = 1e300, pc_err = 0.0;
         int iters = 1;
-        while (true) {
-            cudaMemsetAsync(s->d_red, 0, 3 * sizeof(unsigned long long), st);
-            for (int node = 1; node < 8; node++) {
-                sh_k_predict<<<blocks, tpb, 0, st>>>(W, n, node, hstep);
-                ag_launch_forces_table(E, c, s->t + (s->tc + hstep * h_nodes[node]), io, st);
-                sh_k_update<<<blocks, tpb, 0, st>>>(W, n, n_real, node, s->d_red);
-                out->evals++;
-            }
-            cudaMemcpyAsync(red, s->d_red, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        if (nb == 1) {
+            /* one block: the whole predictor-corrector loop in one launch */
+            sh_k_step<<<1, tpb, sizeof(ShStepSmem), st>>>(E.self_dev, c, A);
+            if (ag_cuda_check(cudaGetLastError(), "IAS15 step kernel")) return 1;
+            cudaMemcpyAsync(red, s->d_red, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
             cudaMemcpyAsync(&hstat, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
-            if (ag_cuda_check(cudaStreamSynchronize(st), "IAS15 iteration")) return 1;
-            if (hstat != 0) { out->status = hstat; break; }
-            double mdb, ma;
-            std::memcpy(&mdb, &red[0], 8);
-            std::memcpy(&ma, &red[1], 8);
-            pc_err = mdb / ma;
-            const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
-            if (conv) break;
-            pc_last = pc_err;
-            iters++;
+            if (ag_cuda_check(cudaStreamSynchronize(st), "IAS15 step")) return 1;
+            iters = (int)red[3];
+            out->evals += 1 + 7 * (long long)iters;
+            if (hstat != 0) out->status = hstat;
+        } else {
+            out->evals++;
+            double pc_last = 1e300, pc_err = 0.0;
+            while (true) {
+                cudaMemsetAsync(s->d_red, 0, 3 * sizeof(unsigned long long), st);
+                sh_k_step<<<nb, tpb, sizeof(ShStepSmem), st>>>(E.self_dev, c, A);
+                if (ag_cuda_check(cudaGetLastError(), "IAS15 step kernel")) return 1;
+                A.first = 0;
+                out->evals += 7;
+                cudaMemcpyAsync(red, s->d_red, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+                cudaMemcpyAsync(&hstat, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
+                if (ag_cuda_check(cudaStreamSynchronize(st), "IAS15 iteration")) return 1;
+                if (hstat != 0) { out->status = hstat; break; }
+                double mdb, ma;
+                std::memcpy(&mdb, &red[0], 8);
+                std::memcpy(&ma, &red[1], 8);
+                pc_err = mdb / ma;
+                const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
+                if (conv) break;
+                pc_last = pc_err;
+                iters++;
+            }
         }
         if (out->status) break;
         out->iterations += iters;

@@ -162,6 +162,28 @@ def test_shared_step_drop_in_vs_oracle(synth_files):
     ex.detach(sim); sim.free()
 
 
+@pytest.mark.parametrize("n", [1, 200])
+def test_shared_step_past_coverage_sets_status(golden_paths, n):
+    """A drop-in integration that runs past the ephemeris' end stops with
+    ASSIST's coverage error at a time still inside the coverage, with one step
+    kernel block (1 particle: the whole corrector loop in one launch) and with
+    two (200 particles: one launch per iteration)."""
+    from assist_gb300 import Extras, Simulation
+    eph = _eph(golden_paths)
+    tb, te = eph.time_bounds()
+    sim = Simulation.create(); ex = Extras(sim, eph)
+    rng = np.random.default_rng(3)
+    for _ in range(n):
+        a = rng.uniform(2.2, 3.2)
+        sim.add(a, 0.0, 0.0, 0.0, 0.01720209895 / np.sqrt(a), 0.0)
+    sim.t = te - 40.0
+    sim.integrate(te + 40.0)
+    assert sim.status == 1 and b"coverage" in sim.error_message
+    assert te - 40.0 < sim.t <= te
+    assert np.isfinite([sim.particle(i).x for i in range(n)]).all()
+    ex.detach(sim); sim.free()
+
+
 def test_shared_step_roundtrip(synth_files):
     """Mirror of the reference's unit_tests/roundtrip_adaptive_*: forward and back."""
     from assist_gb300 import Extras, Simulation, synth

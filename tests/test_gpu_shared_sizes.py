@@ -54,7 +54,10 @@ def test_shared_step_1024_main_belt_one_year(synth_files):
     print("1024 main-belt, one year, shared step: %d steps; |dx| median %.2e max %.2e AU"
           % (sim.steps_done, np.median(dx), dx.max()))
     assert dx.max() < 1e-9
-    assert sim.steps_done == info["accepted"]
+    # the step size comes from maxima over 1,024 particles whose last bits
+    # differ between the device's summation orders and the oracle's: the
+    # step before the end can come out either side of it
+    assert abs(sim.steps_done - info["accepted"]) <= 1
     ex.detach(sim); sim.free()
 
 

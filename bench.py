@@ -34,7 +34,11 @@ integrated from t0 to its t_end by the persistent kernel.
   configs : the batched mixed-length population (65,536 particles, lengths
           logU[30 d, 10 yr]) and the variational population (1,048,576
           particles x 6 variational particles, lengths logU[30 d, 5 yr], 1% on
-          close Earth approaches), each timed with an oracle parity sample.
+          close Earth approaches), each timed with an oracle parity sample;
+          and the shared-step drop-in (one REBOUND simulation through
+          sim.integrate) at 1,024 main-belt particles over one year and at
+          4,096 NEOs x 6 variational particles over ten years and back, each
+          beside the oracle's shared-step IAS15 on one CPU thread.
 
 --impl reference times that CPU path alone (the reference arm); it loads no
 part of this library.  Multi-GPU (torchrun): weak scaling, each rank
@@ -347,6 +351,131 @@ def extra_config(name, desc, batch, eph, o_cpu, pop, opts, steps, warmup, stream
             "parity_oracle_s": cpu_s}
 
 
+def _dropin_sim(eph, state, var_tp=()):
+    """One REBOUND simulation with ASSIST attached (the drop-in surface):
+    real particles, then unit-deviation variational particles in x, y, z,
+    vx, vy, vz order for each entry of var_tp."""
+    from assist_gb300 import Extras, Simulation
+    sim = Simulation.create()
+    ex = Extras(sim, eph)
+    for s in state:
+        sim.add(*s)
+    for k, i in enumerate(var_tp):
+        p = sim.particle(sim.add_variation(int(i)))
+        setattr(p, ["x", "y", "z", "vx", "vy", "vz"][k % 6], 1.0)
+    sim.t = T0
+    return sim, ex
+
+
+def _dropin_run(sim, t1, budget_s, chunk=365.25):
+    """sim.integrate(t1) in chunks of simulated time: wall seconds, or None
+    when past budget_s (one shared step is as small as the smallest any
+    particle asks for)."""
+    start = time.perf_counter()
+    d = 1.0 if t1 >= sim.t else -1.0
+    while sim.t != t1:
+        nxt = sim.t + d * chunk
+        sim.integrate(t1 if d * (nxt - t1) >= 0 else nxt)
+        if sim.status != 0 or time.perf_counter() - start > budget_s:
+            return None
+    return time.perf_counter() - start
+
+
+def shared_configs(eph, system, o_cpu, runs):
+    """The shared-step drop-in at its two configuration sizes, through the
+    REBOUND/ASSIST surface (host particles in, host particles out, the host's
+    step control around the device's step kernel): wall time of
+    sim.integrate, parity with the oracle's shared-step IAS15 (the same
+    method on the CPU, one thread, timed as the CPU baseline)."""
+    synth = _synth()
+    AU_M = 149597870700.0
+    out = []
+    # 1,024 main-belt particles, one year
+    pop = synth.population(system, "mba", 1024, seed=SEED_POP + 10, t0=T0)
+    sim, ex = _dropin_sim(eph, pop.state)
+    _dropin_run(sim, T0 + 30.0, 60.0)                 # untimed: first use of the step kernel
+    ex.detach(sim); sim.free()
+    walls, steps = [], 0
+    for _ in range(runs):
+        sim, ex = _dropin_sim(eph, pop.state)
+        w = _dropin_run(sim, T0 + LENGTH, 120.0)
+        steps = sim.steps_done
+        g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+        ex.detach(sim); sim.free()
+        if w is None:
+            break
+        walls.append(w)
+    t = time.perf_counter()
+    r, _, info = o_cpu.integrate(T0, T0 + LENGTH, pop.state)
+    cpu_s = time.perf_counter() - t
+    dx = np.abs(g[:, :3] - r[:, :3]).max(axis=1)
+    pdays = 1024 * LENGTH
+    out.append({"name": "shared-step-1024-main-belt-1yr",
+                "description": "one REBOUND simulation of 1,024 main-belt particles sharing the IAS15 step "
+                               "(epsilon 1e-9), 365.25 days, through sim.integrate with ASSIST attached",
+                "n_particles": 1024, "value": pdays / np.mean(walls) if walls else None, "unit": UNIT,
+                "wall_s": float(np.mean(walls)) if walls else None, "runs": len(walls), "steps": int(steps),
+                "us_per_step": 1e6 * float(np.mean(walls)) / max(steps, 1) if walls else None,
+                "parity": {"max_au": float(dx.max()), "median_au": float(np.median(dx)),
+                           "oracle_steps": info["accepted"]},
+                "cpu_baseline": {"value": pdays / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                                 "us_per_step": 1e6 * cpu_s / max(info["accepted"], 1),
+                                 "sample": "the whole configuration: the oracle's shared-step IAS15, %.1f s" % cpu_s}})
+    # 4,096 NEOs x 6 variational particles, ten years forward and back
+    n = 4096
+    pop = synth.population(system, "neo", n, seed=33, t0=T0)
+    var_tp = np.repeat(np.arange(n), 6)
+    sim, ex = _dropin_sim(eph, pop.state, var_tp)
+    w_f = _dropin_run(sim, T0 + 3652.5, 300.0)
+    steps_f = sim.steps_done
+    w_b = None
+    if w_f is not None:
+        sim.dt = -sim.dt
+        w_b = _dropin_run(sim, T0, 300.0)
+    steps_b = sim.steps_done - steps_f
+    g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+    ex.detach(sim); sim.free()
+    line = {"name": "shared-step-4096-neo-x6-variational-10yr-roundtrip",
+            "description": "one REBOUND simulation of 4,096 NEOs (seed 33: no impactor over the ten years), each "
+                           "with 6 variational particles (unit deviations), sharing the IAS15 step: 10 years forward, "
+                           "then back to the start; value counts real particle-days both ways",
+            "n_particles": n, "n_var_per_particle": 6, "unit": UNIT, "steps_forward": int(steps_f),
+            "steps_back": int(steps_b)}
+    if w_f is not None and w_b is not None:
+        wall = w_f + w_b
+        dxm = np.abs(g[:n, :3] - pop.state[:, :3]).max(axis=1) * AU_M
+        var0 = np.tile(np.eye(6), (n, 1))
+        dv = np.abs(g[n:] - var0).reshape(n, 6, 6).max(axis=(1, 2))
+        line.update({"value": 2 * n * 3652.5 / wall, "wall_s": wall,
+                     "us_per_step": 1e6 * wall / max(steps_f + steps_b, 1),
+                     "roundtrip": {"position_median_m": float(np.median(dxm)), "position_max_m": float(dxm.max()),
+                                   "variational_identity_median": float(np.median(dv)),
+                                   "variational_identity_max": float(dv.max())}})
+    else:
+        line.update({"value": None, "unfinished": "past its wall budget or a status"})
+    # parity and CPU baseline: the first 10 days against the oracle
+    sim, ex = _dropin_sim(eph, pop.state, var_tp)
+    sim.integrate(T0 + 10.0)
+    g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+    gsteps = sim.steps_done
+    ex.detach(sim); sim.free()
+    t = time.perf_counter()
+    r, rv, info = o_cpu.integrate(T0, T0 + 10.0, pop.state, var_state=np.tile(np.eye(6), (n, 1)),
+                                  var_tp=var_tp.astype(np.int32))
+    cpu_s = time.perf_counter() - t
+    rel = np.abs(g[n:] - rv).reshape(n, 6, 6).max(axis=(1, 2)) / np.abs(rv).reshape(n, 6, 6).max(axis=(1, 2))
+    line["parity_first_10_days"] = {"max_au": float(np.abs(g[:n, :3] - r[:, :3]).max()),
+                                    "variational_rel_max": float(rel.max()), "steps": int(gsteps),
+                                    "oracle_steps": info["accepted"]}
+    line["cpu_baseline"] = {"value": n * 10.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                            "us_per_step": 1e6 * cpu_s / max(info["accepted"], 1),
+                            "sample": "the first 10 days (steps there are shorter than the ten-year average: "
+                                      "compare us_per_step), the oracle's shared-step IAS15 with the variational "
+                                      "particles, %.1f s" % cpu_s}
+    out.append(line)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -559,6 +688,7 @@ def main():
             batch, eph, o_cpu, p4, batch.options(group_steps=2, warm_start=w4), 1, 1, stream, flush, dev, 512,
             threads, var=v4))
         del p4, v4
+        configs.extend(shared_configs(eph, system, o_cpu, 3))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded .440/SPK ephemeris, seeded population)",

@@ -197,9 +197,8 @@ struct ShStepSmem {
 
 /* Accelerations of the block's particles at node n (table S.tab[n]) into
  * io.a; ends with a block barrier. */
-__device__ __forceinline__ void sh_step_forces(ShStepSmem& S, const ShStepArgs& A, const DevEphem& E, const ForceCfg& c,
-                                               int n, bool jac, int v0, int v1) {
-    const AgForceIO& io = A.io;
+__device__ __forceinline__ void sh_step_forces(ShStepSmem& S, const AgForceIO& io, const int* vowner, const DevEphem& E,
+                                               const ForceCfg& c, int n, bool jac, int v0, int v1) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, r0 = 32 * blockIdx.x;
     const int ir = r0 + lane;
     const bool live = ir < io.n_real;
@@ -244,7 +243,7 @@ __device__ __forceinline__ void sh_step_forces(ShStepSmem& S, const ShStepArgs& 
     if (jac) {
         __syncthreads();
         for (int q = v0 + tid; q < v1; q += blockDim.x) {
-            const int p = io.var_index[q], l = A.vowner[q] - r0;
+            const int p = io.var_index[q], l = vowner[q] - r0;
             const int cfg = io.var_cfg ? io.var_cfg[q] : -1;
             double J[3][6], JA[3][3];
             for (int a = 0; a < 3; a++) {
@@ -271,11 +270,12 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
     ShStepSmem& S = *reinterpret_cast<ShStepSmem*>(sh_smem);
     const DevEphem& E = *Ep;
     const ShView& W = A.W;
+    const AgForceIO& io = A.io;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nt = blockDim.x;
     const int q0 = 3 * A.pstart[blockIdx.x], q1 = 3 * A.pstart[blockIdx.x + 1];   /* (particle, component) tasks */
-    const int n_real = A.io.n_real, r0 = 32 * blockIdx.x, r1 = min(r0 + 32, n_real);
-    const int v0 = (A.io.var_start && r0 < r1) ? A.io.var_start[r0] : 0;
-    const int v1 = (A.io.var_start && r0 < r1) ? A.io.var_start[r1] : 0;
+    const int n_real = io.n_real, r0 = 32 * blockIdx.x, r1 = min(r0 + 32, n_real);
+    const int v0 = (io.var_start && r0 < r1) ? io.var_start[r0] : 0;
+    const int v1 = (io.var_start && r0 < r1) ? io.var_start[r1] : 0;
     const bool jac = v1 > v0;                    /* block-uniform */
     const bool single = gridDim.x == 1;
     if (A.first) {
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
         bad = __syncthreads_or(bad);
         if (bad) {
             if (tid == 0) {
-                if (n_real > 0) atomicMax(A.io.status, (int)AG_ERR_COVERAGE);
+                if (n_real > 0) atomicMax(io.status, (int)AG_ERR_COVERAGE);
                 if (single) { A.red[0] = A.red[1] = A.red[2] = 0ull; A.red[3] = 1ull; }
             }
             return;
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
         /* node 0: the start of the step */
         for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, 0, A.hstep);
         __syncthreads();
-        sh_step_forces(S, A, E, c, 0, jac, v0, v1);
+        sh_step_forces(S, io, A.vowner, E, c, 0, jac, v0, v1);
         for (int q = q0 + tid; q < q1; q += nt) sh_start(W, A.plist[q / 3], q % 3);
     } else {
         const double* src = reinterpret_cast<const double*>(A.gtab);
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
         for (int node = 1; node < 8; node++) {
             for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, node, A.hstep);
             __syncthreads();
-            sh_step_forces(S, A, E, c, node, jac, v0, v1);
+            sh_step_forces(S, io, A.vowner, E, c, node, jac, v0, v1);
             for (int q = q0 + tid; q < q1; q += nt) sh_update(W, A.plist[q / 3], q % 3, n_real, node, mdb, ma, mb);
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -367,10 +367,12 @@ static int sh_step_attr(void) {
     return (int)e;
 }
 
-__device__ __forceinline__ void sh_predict_next(const ShView& W, int i, double ratio) {
+/* b and e of component k of particle i for the next step from the last
+ * accepted step's br, er (the shift of the acceleration polynomial by the
+ * step-size ratio; b and e zeroed when the ratio passes 20). */
+__device__ __forceinline__ void sh_predict_next(const ShView& W, int i, int k, double ratio) {
     if (ratio > 20.0) {
-        for (int k = 0; k < 3; k++)
-            for (int q = 0; q < 7; q++) { W(S_E + q, k, i) = 0.0; W(S_B + q, k, i) = 0.0; }
+        for (int q = 0; q < 7; q++) { W(S_E + q, k, i) = 0.0; W(S_B + q, k, i) = 0.0; }
         return;
     }
     double qp[8];
@@ -379,64 +381,64 @@ __device__ __forceinline__ void sh_predict_next(const ShView& W, int i, double r
     constexpr double binom[8][8] = {
         {1, 0, 0, 0, 0, 0, 0, 0}, {1, 1, 0, 0, 0, 0, 0, 0}, {1, 2, 1, 0, 0, 0, 0, 0}, {1, 3, 3, 1, 0, 0, 0, 0},
         {1, 4, 6, 4, 1, 0, 0, 0}, {1, 5, 10, 10, 5, 1, 0, 0}, {1, 6, 15, 20, 15, 6, 1, 0}, {1, 7, 21, 35, 35, 21, 7, 1}};
-    for (int k = 0; k < 3; k++) {
-        double br[7], er[7];
+    double br[7], er[7];
 #pragma unroll
-        for (int q = 0; q < 7; q++) { br[q] = W(S_BR + q, k, i); er[q] = W(S_ER + q, k, i); }
+    for (int q = 0; q < 7; q++) { br[q] = W(S_BR + q, k, i); er[q] = W(S_ER + q, k, i); }
 #pragma unroll
-        for (int j = 0; j < 7; j++) {
-            double s = 0.0;
+    for (int j = 0; j < 7; j++) {
+        double s = 0.0;
 #pragma unroll
-            for (int q = 6; q >= j; q--) s = fma(br[q], binom[q + 1][j + 1], s);
-            const double e = qp[j + 1] * s;
-            W(S_E + j, k, i) = e;
-            W(S_B + j, k, i) = e + (br[j] - er[j]);
-        }
+        for (int q = 6; q >= j; q--) s = fma(br[q], binom[q + 1][j + 1], s);
+        const double e = qp[j + 1] * s;
+        W(S_E + j, k, i) = e;
+        W(S_B + j, k, i) = e + (br[j] - er[j]);
     }
 }
 
+/* Accepted step of size hstep: one thread per particle component.  x and v
+ * advance by the step's quadratures with compensated sums, the start-of-step
+ * state is kept for dense output, then b and e are predicted for a next step
+ * of hstep * ratio. */
 __global__ void sh_k_accept(ShView W, int n, double hstep, double ratio) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, i = t / 3, k = t - 3 * i;
     if (i >= n) return;
     const double h2 = hstep * hstep;
-    for (int k = 0; k < 3; k++) {
-        double b[7];
+    double b[7];
 #pragma unroll
-        for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
-        const double a0 = W(S_A0, k, i);
-        /* keep the start-of-step state for dense output */
-        W(S_PX, k, i) = W(S_X0, k, i) + W(S_XC, k, i);
-        W(S_PV, k, i) = W(S_V0, k, i) + W(S_VC, k, i);
-        W(S_PA, k, i) = a0;
-        double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
-        ix = fma(ix, h2, W(S_V0, k, i) * hstep);
-        double y = ix + W(S_XC, k, i);
-        const double x0 = W(S_X0, k, i);
-        double s = x0 + y;
-        W(S_XC, k, i) = y - (s - x0);
-        W(S_X0, k, i) = s;
-        double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
-        iv = iv * hstep;
-        y = iv + W(S_VC, k, i);
-        const double v0 = W(S_V0, k, i);
-        s = v0 + y;
-        W(S_VC, k, i) = y - (s - v0);
-        W(S_V0, k, i) = s;
+    for (int q = 0; q < 7; q++) b[q] = W(S_B + q, k, i);
+    const double a0 = W(S_A0, k, i);
+    W(S_PX, k, i) = W(S_X0, k, i) + W(S_XC, k, i);
+    W(S_PV, k, i) = W(S_V0, k, i) + W(S_VC, k, i);
+    W(S_PA, k, i) = a0;
+    double ix = b[6] / 72. + b[5] / 56. + b[4] / 42. + b[3] / 30. + b[2] / 20. + b[1] / 12. + b[0] / 6. + a0 / 2.;
+    ix = fma(ix, h2, W(S_V0, k, i) * hstep);
+    double y = ix + W(S_XC, k, i);
+    const double x0 = W(S_X0, k, i);
+    double s = x0 + y;
+    W(S_XC, k, i) = y - (s - x0);
+    W(S_X0, k, i) = s;
+    double iv = b[6] / 8. + b[5] / 7. + b[4] / 6. + b[3] / 5. + b[2] / 4. + b[1] / 3. + b[0] / 2. + a0;
+    iv = iv * hstep;
+    y = iv + W(S_VC, k, i);
+    const double v0 = W(S_V0, k, i);
+    s = v0 + y;
+    W(S_VC, k, i) = y - (s - v0);
+    W(S_V0, k, i) = s;
 #pragma unroll
-        for (int q = 0; q < 7; q++) { W(S_ER + q, k, i) = W(S_E + q, k, i); W(S_BR + q, k, i) = b[q]; }
-    }
-    sh_predict_next(W, i, ratio);
+    for (int q = 0; q < 7; q++) { W(S_ER + q, k, i) = W(S_E + q, k, i); W(S_BR + q, k, i) = b[q]; }
+    sh_predict_next(W, i, k, ratio);
 }
 
+/* Rejected step: b and e from the last accepted step for the retry's size
+ * (zero: none accepted yet, both cleared); one thread per particle component. */
 __global__ void sh_k_reject(ShView W, int n, double ratio, int zero) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, i = t / 3, k = t - 3 * i;
     if (i >= n) return;
     if (zero) {
-        for (int k = 0; k < 3; k++)
-            for (int q = 0; q < 7; q++) { W(S_B + q, k, i) = 0.0; W(S_E + q, k, i) = 0.0; }
+        for (int q = 0; q < 7; q++) { W(S_B + q, k, i) = 0.0; W(S_E + q, k, i) = 0.0; }
         return;
     }
-    sh_predict_next(W, i, ratio);
+    sh_predict_next(W, i, k, ratio);
 }
 
 /* ------------------------------------------------------------------ host side */
@@ -650,7 +652,7 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     if (sh_upload_vars(s, r, params, &io)) return 1;
     ShView W{s->d_ws, s->cap};
     const size_t F = 3 * (size_t)s->cap;
-    const int tpb = 128, blocks = (n + tpb - 1) / tpb, nb = s->nblocks;
+    const int tpb = 128, blocks3 = (3 * n + tpb - 1) / tpb, nb = s->nblocks;
     cudaStream_t st = s->stream;
     double dir = tmax >= r->t ? 1.0 : -1.0;
     /* the host particles are authoritative: upload them every call; keep the
@@ -752,12 +754,12 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
         }
         if (reject) {
             out->rejected++;
-            if (s->dt_last_success != 0.0) sh_k_reject<<<blocks, tpb, 0, st>>>(W, n, dt_new / s->dt_last_success, 0);
-            else sh_k_reject<<<blocks, tpb, 0, st>>>(W, n, 0.0, 1);
+            if (s->dt_last_success != 0.0) sh_k_reject<<<blocks3, tpb, 0, st>>>(W, n, dt_new / s->dt_last_success, 0);
+            else sh_k_reject<<<blocks3, tpb, 0, st>>>(W, n, 0.0, 1);
             dt = dt_new;
             continue;
         }
-        sh_k_accept<<<blocks, tpb, 0, st>>>(W, n, hstep, dt_new / hstep);
+        sh_k_accept<<<blocks3, tpb, 0, st>>>(W, n, hstep, dt_new / hstep);
         out->accepted++;
         {
             const double y = hstep + s->tc;

@@ -162,6 +162,53 @@ def test_shared_step_drop_in_vs_oracle(synth_files):
     ex.detach(sim); sim.free()
 
 
+@pytest.mark.parametrize("n", [8, 40])
+def test_shared_step_nongrav_variational_vs_oracle(synth_files, n):
+    """Shared-step drop-in with Marsden parameters on every real particle and
+    variational particles of three kinds per particle: a state deviation, a
+    deviation of A1 alone and of A2 alone (ASSIST's particle_params rows
+    N_real + v hold the variational particles' parameter deviations).  One
+    step-kernel block (8 particles) and two (40)."""
+    from assist_gb300 import Extras, Simulation, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "neo", n, seed=12, t0=8000.0)
+    rng = np.random.default_rng(4)
+    A = np.zeros((n, 3))
+    A[:, 0] = rng.choice([-1.0, 1.0], n) * 10 ** rng.uniform(-12, -9, n)
+    A[:, 1] = rng.choice([-1.0, 1.0], n) * 10 ** rng.uniform(-12, -9, n)
+    A[:, 2] = 10 ** rng.uniform(-13, -11, n)
+    var_tp = np.repeat(np.arange(n), 3).astype(np.int32)
+    m = var_tp.size
+    var0 = np.zeros((m, 6))
+    dA = np.zeros((m, 3))
+    var0[0::3, 0] = 1.0          # x deviation
+    dA[1::3, 0] = 1.0            # A1 deviation
+    dA[2::3, 1] = 1.0            # A2 deviation
+    sim = Simulation.create(); ex = Extras(sim, eph)
+    for i in range(n):
+        sim.add(*pop.state[i])
+    for k in range(m):
+        p = sim.particle(sim.add_variation(int(var_tp[k])))
+        p.x, p.y, p.z, p.vx, p.vy, p.vz = var0[k]
+    params = np.concatenate([A, dA])
+    ex.particle_params = params.ravel()
+    sim.t = 8000.0
+    sim.integrate(8100.0)
+    assert sim.status == 0 and sim.t == 8100.0
+    g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+    r, rv, info = O.integrate(8000.0, 8100.0, pop.state, var_state=var0, var_tp=var_tp, params=params)
+    assert info["status"] == 0
+    assert np.abs(g[:n, :3] - r[:, :3]).max() < 1e-9
+    scale = np.abs(rv).max(axis=1)
+    assert (scale[1::3] > 0).all() and (scale[2::3] > 0).all()
+    rel = np.abs(g[n:] - rv).max(axis=1) / scale
+    assert rel.max() < 1e-7
+    assert abs(sim.steps_done - info["accepted"]) <= 1
+    ex.detach(sim); sim.free()
+
+
 @pytest.mark.parametrize("n", [1, 200])
 def test_shared_step_past_coverage_sets_status(golden_paths, n):
     """A drop-in integration that runs past the ephemeris' end stops with

@@ -209,6 +209,46 @@ def test_shared_step_nongrav_variational_vs_oracle(synth_files, n):
     ex.detach(sim); sim.free()
 
 
+@pytest.mark.parametrize("n", [6, 48])
+@pytest.mark.parametrize("kind", ["geocentric", "spk-planets"])
+def test_shared_step_frames_and_formats_vs_oracle(synth_files, synth_files_spk, kind, n):
+    """The drop-in's step kernel in ASSIST's geocentric frame (`geocentric =
+    1`: states about the Earth, the Earth's acceleration removed) and with the
+    planets from an SPK file; every third particle carries one variational
+    particle.  One block (6 particles) and two (48)."""
+    from assist_gb300 import Extras, Simulation, synth
+    from tests.oracle_py import Oracle
+    pl, ast, system = synth_files_spk if kind == "spk-planets" else synth_files
+    eph = _eph((pl, ast)); O = Oracle(pl, ast)
+    pop = synth.population(system, "neo", n, seed=24, t0=8000.0)
+    state = pop.state.copy()
+    geo = 1 if kind == "geocentric" else 0
+    if geo:
+        earth = np.array(system.body(3, np.array(8000.0))).reshape(2, 3)
+        state[:, :3] -= earth[0]; state[:, 3:] -= earth[1]
+    var_tp = np.arange(0, n, 3).astype(np.int32)
+    var0 = np.zeros((var_tp.size, 6))
+    var0[np.arange(var_tp.size), np.arange(var_tp.size) % 6] = 1.0
+    sim = Simulation.create(); ex = Extras(sim, eph)
+    ex.geocentric = geo
+    for s in state:
+        sim.add(*s)
+    for k, i in enumerate(var_tp):
+        p = sim.particle(sim.add_variation(int(i)))
+        p.x, p.y, p.z, p.vx, p.vy, p.vz = var0[k]
+    sim.t = 8000.0
+    sim.integrate(8060.0)
+    assert sim.status == 0 and sim.t == 8060.0
+    g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+    r, rv, info = O.integrate(8000.0, 8060.0, state, var_state=var0, var_tp=var_tp, geocentric=geo)
+    assert info["status"] == 0
+    assert np.abs(g[:n, :3] - r[:, :3]).max() < 1e-9
+    rel = np.abs(g[n:] - rv).max(axis=1) / np.abs(rv).max(axis=1)
+    assert rel.max() < 1e-7
+    assert abs(sim.steps_done - info["accepted"]) <= 1
+    ex.detach(sim); sim.free()
+
+
 @pytest.mark.parametrize("n", [1, 200])
 def test_shared_step_past_coverage_sets_status(golden_paths, n):
     """A drop-in integration that runs past the ephemeris' end stops with

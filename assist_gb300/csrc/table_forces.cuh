@@ -3,8 +3,9 @@
  * time (the REBOUND callback assist_additional_forces, src/forces.c:49-173),
  * as block-level device functions: the block builds the body table of that
  * time in shared memory, then each thread evaluates particles.  Used by the
- * one-launch force kernel (kernels_forces.cu) and by the fused shared-step
- * IAS15 kernel for small simulations (kernels_shared.cu).
+ * one-launch force kernel (kernels_forces.cu); the shared-step IAS15 kernel
+ * (kernels_shared.cu) uses its Jacobian application for variational
+ * particles.
  */
 #ifndef ASSIST_GB300_TABLE_FORCES_CUH
 #define ASSIST_GB300_TABLE_FORCES_CUH

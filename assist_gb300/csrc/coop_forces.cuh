@@ -94,14 +94,61 @@ __device__ __forceinline__ int ag_astcomp_fused(const DevEphem& E, int m, int co
     return AG_OK;
 }
 
+/* A value as the unevaluated sum hi + lo of two floats ("double-float",
+ * about 48 significant bits), for arithmetic on the FP32 pipes, which on
+ * GB300 retire 64 lanes for every lane of FP64 work. */
+struct AgF2 {
+    float h, l;
+};
+
 /* A body table of one substep time and, per body, the origin minus the body's
  * position: the particle-independent half of every separation
  * x + (xo - x_body) (src/forces.c), formed once per table rather than once
- * per particle.  Rows 0..10 planets, then the asteroids. */
+ * per particle: the eleven planets in FP64, the asteroids as float pairs (their
+ * FP64 positions stay in T.ast). */
 struct AgCoopTab {
     AgTable T;
-    double rel[AG_NPL + AG_MAX_AST][3];
+    double rel[AG_NPL][3];
+    AgF2 arel[AG_MAX_AST][3];
 };
+
+/* Double-float operations: Knuth's two-sum and Dekker's fast two-sum for
+ * the addition, the product's rounding error from one fused multiply-add,
+ * each result renormalised (the methods of Dekker 1971 and of the
+ * double-double libraries built on them), written with round-to-nearest
+ * intrinsics so that no operation is contracted or reordered. */
+__device__ __forceinline__ AgF2 ag_f2_fast(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ AgF2 ag_f2_add(AgF2 a, AgF2 b) {
+    const float s = __fadd_rn(a.h, b.h);
+    const float bb = __fsub_rn(s, a.h);
+    const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+    return ag_f2_fast(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ AgF2 ag_f2_mul(AgF2 a, AgF2 b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ag_f2_fast(p, e);
+}
+__device__ __forceinline__ AgF2 ag_f2_neg(AgF2 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ AgF2 ag_f2_of(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double ag_f2_to(AgF2 a) { return (double)a.h + (double)a.l; }
+/* 1/sqrt(x): the FP32 estimate y0, then one Newton step in double-float,
+ * y = y0 + y0 (1 - x y0^2) / 2 (relative error about 1.5 e0^2, a few 1e-14). */
+__device__ __forceinline__ AgF2 ag_f2_rsqrt(AgF2 x) {
+    const float y0 = rsqrtf(x.h);
+    const AgF2 y = {y0, 0.0f};
+    const AgF2 t = ag_f2_mul(x, ag_f2_mul(y, y));
+    const AgF2 e = ag_f2_add({1.0f, 0.0f}, ag_f2_neg(t));
+    return ag_f2_add(y, ag_f2_mul(e, {0.5f * y0, 0.0f}));
+}
 
 /* ---- The active .440 record staged in shared memory by a bulk (TMA) copy.
  *
@@ -260,7 +307,7 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
                 const double sun = comp == 0 ? T.P.x[AG_SUN] : (comp == 1 ? T.P.y[AG_SUN] : T.P.z[AG_SUN]);
                 const double xa = S.ast_h[q / 3][comp] + sun;
                 T.ast[q / 3][comp] = xa;
-                if (bary) CT.rel[AG_NPL + q / 3][comp] = 0.0 - xa;
+                if (bary) CT.arel[q / 3][comp] = ag_f2_of(0.0 - xa);
             }
         return;
     }
@@ -283,7 +330,7 @@ __device__ __forceinline__ void ag_coop_table_pass2(const DevEphem& E, const For
             const double sun = S.col[AG_C_SUN][comp] * E.inv_cau;
             const double xa = S.ast_h[task / 3][comp] + sun;
             T.ast[task / 3][comp] = xa;
-            if (bary) CT.rel[AG_NPL + task / 3][comp] = 0.0 - xa;
+            if (bary) CT.arel[task / 3][comp] = ag_f2_of(0.0 - xa);
         }
         int nv = (c.forces & AG_F_EIH) ? c.gr_eih_sources : 0;
         if (c.geocentric) nv = nv > AG_EAR + 1 ? nv : AG_EAR + 1;
@@ -304,8 +351,8 @@ __device__ __forceinline__ void ag_coop_rel_geo(const DevEphem& E, AgCoopTab& CT
     for (int q = tid; q < 3 * (AG_NPL + E.n_ast); q += 128) {
         const int k = q / 3, comp = q % 3;
         const double xo = comp == 0 ? P.x[AG_EAR] : (comp == 1 ? P.y[AG_EAR] : P.z[AG_EAR]);
-        const double xb = k < AG_NPL ? (comp == 0 ? P.x[k] : (comp == 1 ? P.y[k] : P.z[k])) : CT.T.ast[k - AG_NPL][comp];
-        CT.rel[k][comp] = xo - xb;
+        if (k < AG_NPL) CT.rel[k][comp] = xo - (comp == 0 ? P.x[k] : (comp == 1 ? P.y[k] : P.z[k]));
+        else CT.arel[k - AG_NPL][comp] = ag_f2_of(xo - CT.T.ast[k - AG_NPL][comp]);
     }
 }
 
@@ -318,25 +365,76 @@ __device__ __forceinline__ void ag_coop_sep(const AgCoopTab& CT, const double* x
     ri = rsqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
 }
 
+/* Origin minus asteroid m in FP64 (x + this is the separation of
+ * src/forces.c's direct term), from the table's positions. */
+__device__ __forceinline__ void ag_coop_ast_rel(const AgCoopTab& CT, bool geo, int m, double* r) {
+    const AgTable& T = CT.T;
+    if (geo) {
+        r[0] = T.P.x[AG_EAR] - T.ast[m][0]; r[1] = T.P.y[AG_EAR] - T.ast[m][1]; r[2] = T.P.z[AG_EAR] - T.ast[m][2];
+    } else {
+        r[0] = 0.0 - T.ast[m][0]; r[1] = 0.0 - T.ast[m][1]; r[2] = 0.0 - T.ast[m][2];
+    }
+}
+
+/* An asteroid closer than this (AU, squared) to the particle has its term in
+ * FP64: there the float-pair separation's absolute error (about 2^-48 of the
+ * heliocentric distances, 1e-14 AU) would no longer be small against the
+ * separation.  Beyond it the pair term's relative error (a few 1e-13) times the
+ * term's share of the acceleration (below 1.3e-5 for the heaviest asteroid at
+ * 0.02 AU from a main-belt particle) stays below 1e-17. */
+#define AG_AST_NEAR2 4.0e-4f
+
 /* Direct gravity of asteroids m0..m1-1 (src/forces.c, the asteroid loop of
- * the direct term), separations from the table's rel rows. */
+ * the direct term).  Without the Jacobian each term is computed in
+ * double-float arithmetic on the FP32 pipes (the asteroids' terms are below
+ * 1e-4 of the acceleration), except for an asteroid within 0.02 AU of this
+ * particle, and the terms' sum joins the FP64 acceleration at the end; with
+ * the Jacobian every term is FP64. */
 template <bool JAC>
-__device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoopTab& CT, bool on_ast, const double* x,
-                                                  int m0, int m1, double& ax, double& ay, double& az, double (*J)[6]) {
+__device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoopTab& CT, bool geo, bool on_ast,
+                                                  const double* x, int m0, int m1, double& ax, double& ay, double& az,
+                                                  double (*J)[6]) {
+    if (JAC) {
 #pragma unroll 1
-    for (int m = m0; m < m1; m++) {
-        const double ddx = x[0] + CT.rel[AG_NPL + m][0], ddy = x[1] + CT.rel[AG_NPL + m][1],
-                     ddz = x[2] + CT.rel[AG_NPL + m][2];
-        const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
-        const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
-        if (on_ast) { ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az); }
-        if (JAC) {
+        for (int m = m0; m < m1; m++) {
+            double r[3];
+            ag_coop_ast_rel(CT, geo, m, r);
+            const double ddx = x[0] + r[0], ddy = x[1] + r[1], ddz = x[2] + r[2];
+            const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
+            const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
+            if (on_ast) { ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az); }
             const double g5 = 3.0 * gr3 * rinv * rinv;
             const double d[3] = {ddx, ddy, ddz};
             for (int a = 0; a < 3; a++)
                 for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
         }
+        return;
     }
+    if (!on_ast) return;
+    const AgF2 xf[3] = {ag_f2_of(x[0]), ag_f2_of(x[1]), ag_f2_of(x[2])};
+    AgF2 sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f}, sz = {0.0f, 0.0f};
+#pragma unroll 1
+    for (int m = m0; m < m1; m++) {
+        const AgF2 rx = CT.arel[m][0], ry = CT.arel[m][1], rz = CT.arel[m][2];
+        const float ex = xf[0].h + rx.h, ey = xf[1].h + ry.h, ez = xf[2].h + rz.h;
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < AG_AST_NEAR2) {
+            double r[3];
+            ag_coop_ast_rel(CT, geo, m, r);
+            const double ddx = x[0] + r[0], ddy = x[1] + r[1], ddz = x[2] + r[2];
+            const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
+            const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
+            ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az);
+            continue;
+        }
+        const AgF2 dx = ag_f2_add(xf[0], rx), dy = ag_f2_add(xf[1], ry), dz = ag_f2_add(xf[2], rz);
+        const AgF2 r2 = ag_f2_add(ag_f2_mul(dx, dx), ag_f2_add(ag_f2_mul(dy, dy), ag_f2_mul(dz, dz)));
+        const AgF2 ri = ag_f2_rsqrt(r2);
+        const AgF2 g = ag_f2_neg(ag_f2_mul({E.ast_gm_hi[m], E.ast_gm_lo[m]}, ag_f2_mul(ri, ag_f2_mul(ri, ri))));
+        sx = ag_f2_add(sx, ag_f2_mul(g, dx));
+        sy = ag_f2_add(sy, ag_f2_mul(g, dy));
+        sz = ag_f2_add(sz, ag_f2_mul(g, dz));
+    }
+    ax += ag_f2_to(sx); ay += ag_f2_to(sy); az += ag_f2_to(sz);
 }
 
 /* EIH per-source sums (Newtonian acceleration of source j by the other
@@ -430,8 +528,9 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, co
         const bool on_ast = (c.forces & AG_F_AST) != 0;
         const int h = (E.n_ast + 1) / 2;
         if (direct && (on_ast || JAC))
-            ag_coop_asteroids<JAC>(E, CT, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay, az, J);
-        if (JAC && w == 2 && (c.forces & AG_F_EARTH_H)) {
+            ag_coop_asteroids<JAC>(E, CT, c.geocentric == 1, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay,
+                                   az, J);
+        if (w == 2 && (c.forces & AG_F_EARTH_H)) {
             double dx, dy, dz, ri;
             ag_coop_sep(CT, x, AG_EAR, dx, dy, dz, ri);
             ag_term_earth_h<JAC>(E, c, dx, dy, dz, ri, ax, ay, az, J);
@@ -494,8 +593,6 @@ __device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoop
                     ag_term_planet<false>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, nullptr);
                 }
             }
-            if (c.forces & AG_F_EARTH_H)
-                ag_term_earth_h<false>(E, c, dx[AG_EAR], dy[AG_EAR], dz[AG_EAR], ri[AG_EAR], ax, ay, az, nullptr);
             if (c.geocentric == 1) { ax -= ao[0]; ay -= ao[1]; az -= ao[2]; }
         } else {
             if (c.forces & AG_F_EIH) ag_term_eih<TableBodies, false>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, nullptr);

@@ -68,6 +68,7 @@ struct DevEphem {
     const double* spk;           /* the whole SPK file as doubles */
     long long spk_ndbl;
     double ast_beg[AG_MAX_AST], ast_end[AG_MAX_AST], ast_res[AG_MAX_AST], ast_gm[AG_MAX_AST];
+    float ast_gm_hi[AG_MAX_AST], ast_gm_lo[AG_MAX_AST];   /* ast_gm as a float pair hi + lo */
     int ast_nseg[AG_MAX_AST], ast_seg0[AG_MAX_AST];
     const struct AgSpkSeg* segs; /* per segment, see AgSpkSeg */
     const AgRecMeta* rec_meta;     /* per SPK record: (MID as JD, RADIUS/86400, 86400/RADIUS, 0) */

@@ -463,6 +463,8 @@ static int ag_finish_view(const struct assist_ephem* e, DevEphem& D, DevEphem* o
         for (int m = 0; m < D.n_ast; m++) {
             const spk_target_h& t = s->targets[(size_t)m];
             D.ast_beg[m] = t.beg; D.ast_end[m] = t.end; D.ast_res[m] = t.res; D.ast_gm[m] = t.mass;
+            D.ast_gm_hi[m] = (float)t.mass;
+            D.ast_gm_lo[m] = (float)(t.mass - (double)D.ast_gm_hi[m]);
             D.ast_nseg[m] = (int)t.one.size();
             D.ast_seg0[m] = s->seg0[(size_t)m];
         }

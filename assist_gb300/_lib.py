@@ -112,6 +112,9 @@ clib.assist_gb300_warm_log_count.restype = c_int
 clib.assist_gb300_forces_device.argtypes = [c_void_p, POINTER(Options), c_int, c_void_p, c_void_p, c_void_p, c_int,
                                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_forces_device.restype = c_int
+clib.assist_gb300_forces_shared_time_device.argtypes = [c_void_p, POINTER(Options), c_int, c_double, c_void_p, c_void_p,
+                                                        c_void_p, c_void_p, c_void_p]
+clib.assist_gb300_forces_shared_time_device.restype = c_int
 clib.assist_gb300_ephem_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
 clib.assist_gb300_ephem_device.restype = c_int
 clib.assist_gb300_encounter_ratio_device.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]

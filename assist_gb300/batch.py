@@ -192,6 +192,24 @@ def forces_device(ephem: Ephem, t, state, params=None, var_state=None, acc=None,
     return acc, var_acc
 
 
+def forces_shared_time_device(ephem: Ephem, t: float, state, params=None, acc=None, status=None,
+                              opts: Optional[Options] = None, stream=None):
+    """One force evaluation of n particles at one time t (torch CUDA tensors)
+    by the block-cooperative evaluation of the batched and shared-step
+    integrators."""
+    import torch
+    o = opts or options()
+    n = state.shape[0]
+    if acc is None:
+        acc = torch.empty((n, 3), dtype=torch.float64, device=state.device)
+    s = None if stream is None else c_void_p(stream.cuda_stream)
+    rc = clib.assist_gb300_forces_shared_time_device(byref(ephem), byref(o), n, float(t), _ptr(state), _ptr(params),
+                                                     _ptr(acc), _ptr(status), s)
+    if rc != 0:
+        raise RuntimeError("assist_gb300_forces_shared_time_device failed (%d): %s" % (rc, last_error()))
+    return acc
+
+
 def bodies_device(ephem: Ephem, t, out=None, status=None, stream=None):
     """All bodies at n times: (n, n_bodies, 10) = GM, x, v, a (torch CUDA)."""
     import torch

@@ -577,6 +577,21 @@ extern "C" int assist_gb300_forces_device(const struct assist_ephem* e, const st
     return ASSIST_SUCCESS;
 }
 
+extern "C" int assist_gb300_forces_shared_time_device(const struct assist_ephem* e, const struct assist_gb300_options* o,
+                                                      int n, double t, const double* d_state, const double* d_params,
+                                                      double* d_acc, int* d_status, void* stream) {
+    if (n < 0 || (n > 0 && (!d_state || !d_acc))) { ag_set_error("invalid arguments"); return ASSIST_ERROR_N; }
+    if (n == 0) return ASSIST_SUCCESS;
+    DevEphem D;
+    int st = ag_ephem_device(e, &D);
+    if (st) return st;
+    const ForceCfg c = make_cfg(o->forces, o->gr_eih_sources, o->geocentric, o->alpha, o->nk, o->nm, o->nn, o->r0);
+    if (ag_cuda_check((cudaError_t)ag_launch_forces_coop(D, c, n, t, d_state, d_params, d_acc, d_status,
+                                                         (cudaStream_t)stream), "force kernel (shared time)"))
+        return ASSIST_ERROR_EPHEM_FILE;
+    return ASSIST_SUCCESS;
+}
+
 struct BatchScratch {
     int* d_grp = nullptr;           /* grp_start then grp_size */
     int grp_cap = 0;

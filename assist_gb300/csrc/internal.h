@@ -78,6 +78,9 @@ struct AgBatchArgs {
 
 /* launchers (kernels_forces.cu, kernels_ias15.cu) */
 int ag_launch_forces_table(const DevEphem& E, const ForceCfg& c, double t, const AgForceIO& io, cudaStream_t s);
+/* n particles (state n x 6) at one time t, block-cooperative evaluation (kernels_shared.cu) */
+int ag_launch_forces_coop(const DevEphem& E, const ForceCfg& c, int n, double t, const double* state,
+                          const double* params, double* acc, int* status, cudaStream_t s);
 int ag_launch_forces_each(const DevEphem& E, const ForceCfg& c, int n, const double* t, const double* state,
                           const double* params, int nv, const double* var_state, double* acc, double* var_acc,
                           int* status, cudaStream_t s);

@@ -441,6 +441,67 @@ __global__ void sh_k_reject(ShView W, int n, double ratio, int zero) {
     sh_predict_next(W, i, k, ratio);
 }
 
+/* All particles at one time t with the block-cooperative evaluation: block b
+ * takes particles [32 b, 32 b + 32) (state n x 6, params n x 3 or null),
+ * builds the table of t and splits each particle's terms over its four
+ * warps; the partial sums are added ((w3 + w2) + w1) + w0 as in the step
+ * kernel. */
+__global__ void __launch_bounds__(128) sh_k_forces_coop(const DevEphem* __restrict__ Ep, ForceCfg c, int n, double t,
+                                                        const double* __restrict__ state,
+                                                        const double* __restrict__ params, double* acc, int* status) {
+    extern __shared__ __align__(16) unsigned char sh_smem[];
+    ShStepSmem& S = *reinterpret_cast<ShStepSmem*>(sh_smem);
+    const DevEphem& E = *Ep;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int i = 32 * blockIdx.x + lane;
+    const bool live = i < n;
+    AgStageCursor cur;
+    int stage_fail = 0;
+    int bad = ag_coop_table_pass1<false>(E, c, t, S.scr, S.tab[0], tid, nullptr, cur, &stage_fail);
+    bad = __syncthreads_or(bad);
+    if (bad) {
+        if (status && tid < 32 && live) status[i] = AG_ERR_COVERAGE;
+        return;
+    }
+    ag_coop_table_pass2(E, c, t, S.tab[0], S.scr, tid);
+    __syncthreads();
+    if (c.geocentric == 1) { ag_coop_rel_geo(E, S.tab[0], tid); __syncthreads(); }
+    if (wid == 1 && (c.forces & AG_F_EIH)) ag_coop_eih_sources(E, c, S.tab[0].T, lane);
+    __syncthreads();
+    double x[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0}, prm[3] = {0.0, 0.0, 0.0};
+    const double* Ap = nullptr;
+    if (live) {
+        for (int k = 0; k < 3; k++) { x[k] = state[6 * (size_t)i + k]; v[k] = state[6 * (size_t)i + 3 + k]; }
+        if (params) { prm[0] = params[3 * (size_t)i]; prm[1] = params[3 * (size_t)i + 1]; prm[2] = params[3 * (size_t)i + 2]; Ap = prm; }
+    }
+    double a[3] = {0.0, 0.0, 0.0};
+    if (wid < 2) ag_coop_force_split01(wid, live, S.seps, lane, S.tab[0], E, c, x, v, Ap, a);
+    else if (live) ag_coop_force_part<false>(wid, S.tab[0], E, c, x, v, Ap, a, nullptr);
+    if (live) { S.pa[wid][0][lane] = a[0]; S.pa[wid][1][lane] = a[1]; S.pa[wid][2][lane] = a[2]; }
+    __syncthreads();
+    if (tid < 96 && live) {
+        const int k = wid;
+        acc[3 * (size_t)i + k] = ((S.pa[3][k][lane] + S.pa[2][k][lane]) + S.pa[1][k][lane]) + S.pa[0][k][lane];
+        if (k == 0 && status) status[i] = AG_OK;
+    }
+}
+
+int ag_launch_forces_coop(const DevEphem& E, const ForceCfg& c, int n, double t, const double* state,
+                          const double* params, double* acc, int* status, cudaStream_t s) {
+    if (n <= 0) return 0;
+    static bool done[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!(dev >= 0 && dev < 64 && done[dev])) {
+        const cudaError_t e = cudaFuncSetAttribute(sh_k_forces_coop, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)sizeof(ShStepSmem));
+        if (e != cudaSuccess) return (int)e;
+        if (dev >= 0 && dev < 64) done[dev] = true;
+    }
+    sh_k_forces_coop<<<(n + 31) / 32, 128, sizeof(ShStepSmem), s>>>(E.self_dev, c, n, t, state, params, acc, status);
+    return (int)cudaGetLastError();
+}
+
 /* ------------------------------------------------------------------ host side */
 
 struct AgSharedSim {

@@ -422,6 +422,18 @@ int assist_gb300_forces_device(const struct assist_ephem* ephem, const struct as
                                int n_var, const double* d_var_state,
                                double* d_acc, double* d_var_acc, int* d_status, void* stream);
 
+/* One force evaluation for n particles at ONE time t (device pointers), by
+ * the block-cooperative evaluation the batched and the shared-step
+ * integrators run: one 128-thread block per 32 particles builds the body
+ * table of t once and its four warps split each particle's force terms, the
+ * asteroids' terms in double-float arithmetic (within 1e-16 of the
+ * acceleration).  acc[3i..3i+2] = a(x_i, v_i, t); state n*6, params n*3 or
+ * NULL; status (device, may be NULL) receives ASSIST_ERROR_COVERAGE for every
+ * particle when t is outside the ephemeris.  No variational particles. */
+int assist_gb300_forces_shared_time_device(const struct assist_ephem* ephem, const struct assist_gb300_options* opt,
+                                           int n, double t, const double* d_state, const double* d_params,
+                                           double* d_acc, int* d_status, void* stream);
+
 /* Evaluate all 11+N_ast bodies at n times (device pointers).  out holds, per
  * time, (11+N_ast) records of 10 doubles: GM, x,y,z, vx,vy,vz, ax,ay,az, with
  * the same meaning as assist_all_ephem (asteroid velocity/acceleration NaN).

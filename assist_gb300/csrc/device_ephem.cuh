@@ -116,7 +116,7 @@ __device__ __forceinline__ int ag_subinterval(double tt, int niv, double* fl) {
  * (src/ascii_ephem.c:294-300).  Returns AG_OK or AG_ERR_COVERAGE. */
 __device__ __forceinline__ int ag_planet_record(const DevEphem& E, double t, const double** rec, double* tf) {
     const double jd = E.jd_ref + t;
-    if (jd < E.pl_beg || jd > E.pl_end) return AG_ERR_COVERAGE;
+    if (!(jd >= E.pl_beg && jd <= E.pl_end)) return AG_ERR_COVERAGE;   /* NaN too */
     const double num = E.jd_ref + t - E.pl_beg;
     const uint32_t blk = (uint32_t)(E.pl_inc_pow2 ? num * E.pl_inv_inc : num / E.pl_inc);
     if ((long long)blk + 2 >= (long long)E.pl_nrec) return AG_ERR_COVERAGE;
@@ -191,7 +191,7 @@ __device__ inline int ag_planet_full(const DevEphem& E, int body, double t, doub
  * with ASSIST's fixed 149597870.7. */
 __device__ __forceinline__ int ag_asteroid_pos(const DevEphem& E, int m, double t, double* p) {
     const double jd = E.jd_ref + t;
-    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    if (!(jd >= E.ast_beg[m] && jd <= E.ast_end[m])) return AG_ERR_COVERAGE;   /* NaN too */
     int n = 0;
     if (E.ast_nseg[m] > 1) {
         n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);
@@ -403,7 +403,7 @@ static __device__ __noinline__ int ag_spk_planet(const DevEphem& E, int body, do
     const double jd = E.jd_ref + t;
     out[0] = E.gm[body];
     if (E.ps_nseg[body] <= 0) return AG_ERR_NEPHEM;
-    if (jd < E.ps_beg[body] || jd > E.ps_end[body]) return AG_ERR_COVERAGE;
+    if (!(jd >= E.ps_beg[body] && jd <= E.ps_end[body])) return AG_ERR_COVERAGE;   /* NaN too */
     double u[3], v[3], w[3];
     ag_spk_target_pva(E, body, t, u, v, w);
     if (body == AG_EAR || body == AG_MOO) {
@@ -425,7 +425,7 @@ static __device__ __noinline__ int ag_spk_planet(const DevEphem& E, int body, do
  * (src/spk.c:428-474). */
 __device__ __forceinline__ int ag_asteroid_exact(const DevEphem& E, int m, double t, double* p) {
     const double jd = E.jd_ref + t;
-    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    if (!(jd >= E.ast_beg[m] && jd <= E.ast_end[m])) return AG_ERR_COVERAGE;   /* NaN too */
     int n = 0;
     if (E.ast_nseg[m] > 1) {
         n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);

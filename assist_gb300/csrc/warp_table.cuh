@@ -57,7 +57,7 @@ __device__ __forceinline__ double ag_colcomp_exact(const DevEphem& E, const doub
 /* Per-component asteroid position (AU, heliocentric), exact arithmetic. */
 __device__ __forceinline__ int ag_astcomp_exact(const DevEphem& E, int m, int comp, double t, double* out) {
     const double jd = E.jd_ref + t;
-    if (jd < E.ast_beg[m] || jd > E.ast_end[m]) return AG_ERR_COVERAGE;
+    if (!(jd >= E.ast_beg[m] && jd <= E.ast_end[m])) return AG_ERR_COVERAGE;   /* NaN too */
     int n = 0;
     if (E.ast_nseg[m] > 1) {
         n = (int)((E.jd_ref + t - E.ast_beg[m]) / E.ast_res[m]);

@@ -389,12 +389,14 @@ __device__ __forceinline__ void ag_coop_ast_rel(const AgCoopTab& CT, bool geo, i
  * double-float arithmetic on the FP32 pipes (the asteroids' terms are below
  * 1e-4 of the acceleration), except for an asteroid within 0.02 AU of this
  * particle, and the terms' sum joins the FP64 acceleration at the end; with
- * the Jacobian every term is FP64. */
-template <bool JAC>
+ * the Jacobian, or with F2 off, every term is FP64 (the learned-warm-start
+ * builds: beside the network's registers the float-pair chains made that
+ * kernel 1.8x slower). */
+template <bool JAC, bool F2 = true>
 __device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoopTab& CT, bool geo, bool on_ast,
                                                   const double* x, int m0, int m1, double& ax, double& ay, double& az,
                                                   double (*J)[6]) {
-    if (JAC) {
+    if (JAC || !F2) {
 #pragma unroll 1
         for (int m = m0; m < m1; m++) {
             double r[3];
@@ -403,10 +405,12 @@ __device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoo
             const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
             const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
             if (on_ast) { ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az); }
-            const double g5 = 3.0 * gr3 * rinv * rinv;
-            const double d[3] = {ddx, ddy, ddz};
-            for (int a = 0; a < 3; a++)
-                for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
+            if (JAC) {
+                const double g5 = 3.0 * gr3 * rinv * rinv;
+                const double d[3] = {ddx, ddy, ddz};
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
+            }
         }
         return;
     }
@@ -466,7 +470,7 @@ __device__ __forceinline__ void ag_coop_eih_sources(const DevEphem& E, const For
  * with JAC, partial 3x6 Jacobian; JA_out / ng_out (warp 0, optional) receive
  * the derivative of the non-gravitational term by A1..A3 and whether the term
  * applies. */
-template <bool JAC>
+template <bool JAC, bool F2 = true>
 __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, const DevEphem& E, const ForceCfg& c,
                                                   const double* x, const double* v, const double* A, double* acc,
                                                   double (*J)[6], double (*JA_out)[3] = nullptr,
@@ -528,8 +532,8 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, co
         const bool on_ast = (c.forces & AG_F_AST) != 0;
         const int h = (E.n_ast + 1) / 2;
         if (direct && (on_ast || JAC))
-            ag_coop_asteroids<JAC>(E, CT, c.geocentric == 1, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax, ay,
-                                   az, J);
+            ag_coop_asteroids<JAC, F2>(E, CT, c.geocentric == 1, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax,
+                                       ay, az, J);
         if (w == 2 && (c.forces & AG_F_EARTH_H)) {
             double dx, dy, dz, ri;
             ag_coop_sep(CT, x, AG_EAR, dx, dy, dz, ri);

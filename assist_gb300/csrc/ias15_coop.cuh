@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                     if constexpr (NV == 0)
                         ag_coop_force_split01(wid, live, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                 } else if (live) {
-                    fst = ag_coop_force_part<false>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                    fst = ag_coop_force_part<false, !WARM>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
                 }
                 if (live) {
                     S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                             if constexpr (NV == 0)
                                 ag_coop_force_split01(wid, !conv, S.seps, lane, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                         } else if (!conv) {
-                            ag_coop_force_part<false>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                            ag_coop_force_part<false, !WARM>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
                         }
                         if (!conv) {
                             S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];

@@ -697,6 +697,9 @@ def main():
                        "warm_start": "plain predictor (the default; the learned warm start is measured "
                                      "beside it under learned_warm_start)",
                        "l2": "flushed (256 MB write) between steps", "kernel": "block-cooperative groups (group_steps=2)",
+                       "precision": "FP64 throughout, except the asteroids' direct terms beyond 0.02 AU of the "
+                                    "particle: float pairs (about 48 bits) on the FP32 pipes, below 1e-17 of the "
+                                    "acceleration",
                        "parallelism": "dp%d (independent batches, no collective)" % world},
             # per step: the encounter pilot's two kernels and the IAS15 kernel
             "gpu_launches": 3 * args.steps,

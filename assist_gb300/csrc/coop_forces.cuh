@@ -466,6 +466,16 @@ __device__ __forceinline__ void ag_coop_eih_sources(const DevEphem& E, const For
     __syncwarp();
 }
 
+/* The GR potential / simple models (off in ASSIST's default force set), out of
+ * line so that their code stays out of the hot instruction stream. */
+static __device__ __noinline__ void ag_coop_gr_cold(const DevEphem& E, const ForceCfg& c, const double* p, double ri,
+                                                    const double* pv, double* a) {
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    if (c.forces & AG_F_GR_POT) ag_term_gr_pot<false>(E, p, ri, ax, ay, az, nullptr);
+    if (c.forces & AG_F_GR_SIMPLE) ag_term_gr_simple<false>(E, p, ri, pv, ax, ay, az, nullptr);
+    a[0] += ax; a[1] += ay; a[2] += az;
+}
+
 /* Warp w's share of the force evaluation at (x, v): partial acceleration and,
  * with JAC, partial 3x6 Jacobian; JA_out / ng_out (warp 0, optional) receive
  * the derivative of the non-gravitational term by A1..A3 and whether the term
@@ -602,11 +612,10 @@ __device__ __forceinline__ void ag_coop_force_split01(int w, bool active, AgCoop
             if (c.forces & AG_F_EIH) ag_term_eih<TableBodies, false>(B, E, c, P, dx, dy, dz, ri, v, vo, ao, ax, ay, az, nullptr);
             if (c.forces & (AG_F_GR_POT | AG_F_GR_SIMPLE)) {
                 const double p[3] = {dx[AG_SUN], dy[AG_SUN], dz[AG_SUN]};
-                if (c.forces & AG_F_GR_POT) ag_term_gr_pot<false>(E, p, ri[AG_SUN], ax, ay, az, nullptr);
-                if (c.forces & AG_F_GR_SIMPLE) {
-                    const double pv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
-                    ag_term_gr_simple<false>(E, p, ri[AG_SUN], pv, ax, ay, az, nullptr);
-                }
+                const double pv[3] = {v[0] + (vo[0] - P.vx[AG_SUN]), v[1] + (vo[1] - P.vy[AG_SUN]), v[2] + (vo[2] - P.vz[AG_SUN])};
+                double a[3] = {ax, ay, az};
+                ag_coop_gr_cold(E, c, p, ri[AG_SUN], pv, a);
+                ax = a[0]; ay = a[1]; az = a[2];
             }
         }
     }

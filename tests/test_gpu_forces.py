@@ -149,7 +149,8 @@ def test_drop_in_coverage_error_sets_status(golden_paths, dev):
     ex.detach(sim); sim.free()
 
 
-@pytest.mark.parametrize("case", ["default", "nongrav", "geocentric", "eih3", "spk-planets", "no-asteroids"])
+@pytest.mark.parametrize("case", ["default", "nongrav", "geocentric", "eih3", "spk-planets", "no-asteroids",
+                                  "gr-potential", "gr-simple"])
 def test_shared_time_cooperative_forces_vs_oracle(synth_files, synth_files_spk, dev, case):
     """The block-cooperative evaluation the batched and shared-step kernels
     run (assist_gb300_forces_shared_time_device: four warps split each
@@ -185,6 +186,10 @@ def test_shared_time_cooperative_forces_vs_oracle(synth_files, synth_files_spk, 
         kw["gr_eih_sources"] = 3
     if case == "no-asteroids":
         kw["forces"] = 0x7F & ~0x04
+    if case == "gr-potential":
+        kw["forces"] = (0x7F & ~0x40) | 0x100
+    if case == "gr-simple":
+        kw["forces"] = (0x7F & ~0x40) | 0x80
     o = batch.options(**kw)
     st = torch.tensor(state, device=dev)
     prm = torch.tensor(params, device=dev)

@@ -442,16 +442,30 @@ __device__ __forceinline__ void ag_term_eih_core(const Bodies& B, const DevEphem
                 dfac[3 + a] = 2.0 * oc2 * v[a] - 4.0 * oc2 * vj[a];
             }
             const double t8d = -GMj * rj * r2i * 3.5;
+            /* d acc_a / dx_b = -d_a (dpre_b factor + pre dfac_b) - pre factor delta_ab
+             *                 + oc2 rel_a (dpre_b f + pre fv_b) + oc2 t8d aj_a d_b   (term 7 and term 8)
+             * d acc_a / dv_b = -pre d_a dfac_(3+b) + oc2 (4 pre d_b rel_a + pf delta_ab)
+             * as sums of outer products: the row factors d, rel, aj times the
+             * column vectors u, w, y (position) and p, q (velocity). */
+            const double sdu = -dpre_s * factor, swd = oc2 * dpre_s * f, swf = oc2 * pre, sy = oc2 * t8d,
+                         sq = 4.0 * oc2 * pre;
+            double u[3], w[3], y[3], p[3], q[3];
+            for (int b = 0; b < 3; b++) {
+                u[b] = fma(sdu, dj[b], -pre * dfac[b]);
+                w[b] = fma(swd, dj[b], swf * fv[b]);
+                y[b] = sy * dj[b];
+                p[b] = -pre * dfac[3 + b];
+                q[b] = sq * dj[b];
+            }
+            const double diag_x = pre * factor, diag_v = oc2 * pf;
             for (int a = 0; a < 3; a++) {
                 for (int b = 0; b < 3; b++) {
-                    double s = -dpre_s * dj[b] * dj[a] * factor - pre * dj[a] * dfac[b];
-                    if (a == b) s -= pre * factor;
-                    /* d(term7)/dx_b and d(term8)/dx_b, times 1/c^2 */
-                    s += oc2 * (dpre_s * dj[b] * f * rel[a] + pre * fv[b] * rel[a] + t8d * aj[a] * dj[b]);
-                    J[a][b] += s;
-                    double sv = -pre * dj[a] * dfac[3 + b];
-                    sv += oc2 * (pre * 4.0 * dj[b] * rel[a] + (a == b ? pf : 0.0));
-                    J[a][3 + b] += sv;
+                    double s = fma(dj[a], u[b], fma(rel[a], w[b], fma(aj[a], y[b], J[a][b])));
+                    if (a == b) s -= diag_x;
+                    J[a][b] = s;
+                    double sv = fma(dj[a], p[b], fma(rel[a], q[b], J[a][3 + b]));
+                    if (a == b) sv += diag_v;
+                    J[a][3 + b] = sv;
                 }
             }
         }

@@ -384,28 +384,6 @@ __device__ __forceinline__ void ag_coop_ast_rel(const AgCoopTab& CT, bool geo, i
  * 0.02 AU from a main-belt particle) stays below 1e-17. */
 #define AG_AST_NEAR2 4.0e-4f
 
-/* The direct terms' Jacobian (src/forces.c: 3 GM d d^T / r^5 - GM I / r^3 per
- * body) accumulated apart from the other terms': its symmetric part s (xx,
- * xy, xz, yy, yz, zz) and the sum g of GM / r^3, so that a body costs six
- * fused multiply-adds and one addition instead of nine and three;
- * ag_symjac_add then puts s - g I into the partial Jacobian once. */
-struct AgSymJac {
-    double s[6];
-    double g;
-};
-__device__ __forceinline__ void ag_symjac_term(AgSymJac& Y, double gr3, double rk, double d0, double d1, double d2) {
-    const double g5 = 3.0 * gr3 * rk * rk;
-    const double e0 = g5 * d0, e1 = g5 * d1, e2 = g5 * d2;
-    Y.s[0] = fma(e0, d0, Y.s[0]); Y.s[1] = fma(e0, d1, Y.s[1]); Y.s[2] = fma(e0, d2, Y.s[2]);
-    Y.s[3] = fma(e1, d1, Y.s[3]); Y.s[4] = fma(e1, d2, Y.s[4]); Y.s[5] = fma(e2, d2, Y.s[5]);
-    Y.g += gr3;
-}
-__device__ __forceinline__ void ag_symjac_add(const AgSymJac& Y, double (*J)[6]) {
-    J[0][0] += Y.s[0] - Y.g; J[0][1] += Y.s[1]; J[0][2] += Y.s[2];
-    J[1][0] += Y.s[1]; J[1][1] += Y.s[3] - Y.g; J[1][2] += Y.s[4];
-    J[2][0] += Y.s[2]; J[2][1] += Y.s[4]; J[2][2] += Y.s[5] - Y.g;
-}
-
 /* Direct gravity of asteroids m0..m1-1 (src/forces.c, the asteroid loop of
  * the direct term).  Without the Jacobian each term is computed in
  * double-float arithmetic on the FP32 pipes (the asteroids' terms are below
@@ -538,10 +516,7 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, co
             for (int q = 0; q < AG_NPL; q++) {
                 const int k = ag_planet_order(q);
                 const bool on = (k == AG_SUN) ? (c.forces & AG_F_SUN) : (c.forces & AG_F_PLANETS);
-                /* ag_term_planet's acceleration, its Jacobian into Y */
-                const double gr3 = E.gm[k] * ri[k] * ri[k] * ri[k];
-                if (on) { ax = fma(-gr3, dx[k], ax); ay = fma(-gr3, dy[k], ay); az = fma(-gr3, dz[k], az); }
-                if (JAC) ag_symjac_term(Y, gr3, ri[k], dx[k], dy[k], dz[k]);
+                ag_term_planet<JAC>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, &Y);
             }
             if (JAC) ag_symjac_add(Y, J);
         }

@@ -535,13 +535,35 @@ __device__ __forceinline__ void ag_term_gr_simple(const DevEphem& E, const doubl
     }
 }
 
+/* The direct terms' Jacobian (src/forces.c: 3 GM d d^T / r^5 - GM I / r^3 per
+ * body) accumulated apart from the other terms': its symmetric part s (xx,
+ * xy, xz, yy, yz, zz) and the sum g of GM / r^3, so that a body costs six
+ * fused multiply-adds and one addition instead of nine and three;
+ * ag_symjac_add then puts s - g I into the Jacobian once. */
+struct AgSymJac {
+    double s[6];
+    double g;
+};
+__device__ __forceinline__ void ag_symjac_term(AgSymJac& Y, double gr3, double rk, double d0, double d1, double d2) {
+    const double g5 = 3.0 * gr3 * rk * rk;
+    const double e0 = g5 * d0, e1 = g5 * d1, e2 = g5 * d2;
+    Y.s[0] = fma(e0, d0, Y.s[0]); Y.s[1] = fma(e0, d1, Y.s[1]); Y.s[2] = fma(e0, d2, Y.s[2]);
+    Y.s[3] = fma(e1, d1, Y.s[3]); Y.s[4] = fma(e1, d2, Y.s[4]); Y.s[5] = fma(e2, d2, Y.s[5]);
+    Y.g += gr3;
+}
+__device__ __forceinline__ void ag_symjac_add(const AgSymJac& Y, double (*J)[6]) {
+    J[0][0] += Y.s[0] - Y.g; J[0][1] += Y.s[1]; J[0][2] += Y.s[2];
+    J[1][0] += Y.s[1]; J[1][1] += Y.s[3] - Y.g; J[1][2] += Y.s[4];
+    J[2][0] += Y.s[2]; J[2][1] += Y.s[4]; J[2][2] += Y.s[5] - Y.g;
+}
+
 /* Direct gravity of asteroids m0..m1-1 (their positions from the Bodies
  * policy); on_ast false keeps only the Jacobian (ASSIST's variational
  * equations include the asteroids even when their force is off). */
 template <class Bodies, bool JAC>
 __device__ __forceinline__ int ag_term_asteroids(const Bodies& B, const DevEphem& E, bool on_ast, const double* x,
                                                  const double* xo, int m0, int m1, double& ax, double& ay, double& az,
-                                                 double (*J)[6]) {
+                                                 AgSymJac* Y) {
 #pragma unroll 1
     for (int m = m0; m < m1; m++) {
         double pa[3];
@@ -551,12 +573,7 @@ __device__ __forceinline__ int ag_term_asteroids(const Bodies& B, const DevEphem
         const double rinv = rsqrt(fma(ddx, ddx, fma(ddy, ddy, ddz * ddz)));
         const double gr3 = E.ast_gm[m] * rinv * rinv * rinv;
         if (on_ast) { ax = fma(-gr3, ddx, ax); ay = fma(-gr3, ddy, ay); az = fma(-gr3, ddz, az); }
-        if (JAC) {
-            const double g5 = 3.0 * gr3 * rinv * rinv;
-            const double d[3] = {ddx, ddy, ddz};
-            for (int a = 0; a < 3; a++)
-                for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
-        }
+        if (JAC) ag_symjac_term(*Y, gr3, rinv, ddx, ddy, ddz);
     }
     return AG_OK;
 }
@@ -564,15 +581,10 @@ __device__ __forceinline__ int ag_term_asteroids(const Bodies& B, const DevEphem
 /* Direct gravity of one planet k; on: its force flag. */
 template <bool JAC>
 __device__ __forceinline__ void ag_term_planet(const DevEphem& E, bool on, int k, double dk0, double dk1, double dk2,
-                                               double rk, double& ax, double& ay, double& az, double (*J)[6]) {
+                                               double rk, double& ax, double& ay, double& az, AgSymJac* Y) {
     const double gr3 = E.gm[k] * rk * rk * rk;
     if (on) { ax = fma(-gr3, dk0, ax); ay = fma(-gr3, dk1, ay); az = fma(-gr3, dk2, az); }
-    if (JAC) {
-        const double g5 = 3.0 * gr3 * rk * rk;
-        const double d[3] = {dk0, dk1, dk2};
-        for (int a = 0; a < 3; a++)
-            for (int b = 0; b < 3; b++) J[a][b] += g5 * d[a] * d[b] - (a == b ? gr3 : 0.0);
-    }
+    if (JAC) ag_symjac_term(*Y, gr3, rk, dk0, dk1, dk2);
 }
 
 /* direct-sum order of the planets, src/forces.c:281-293 */
@@ -643,16 +655,18 @@ __device__ __forceinline__ int ag_forces(Bodies& B, const DevEphem& E, const For
     /* direct Newtonian gravity: asteroids, then planets in ASSIST's order */
     if (c.forces & (AG_F_SUN | AG_F_PLANETS | AG_F_AST)) {
         const bool on_ast = (c.forces & AG_F_AST) != 0;
+        AgSymJac Y = {{0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, 0.0};
         if (on_ast || JAC) {
-            st = ag_term_asteroids<Bodies, JAC>(B, E, on_ast, x, xo, 0, E.n_ast, ax, ay, az, J);
+            st = ag_term_asteroids<Bodies, JAC>(B, E, on_ast, x, xo, 0, E.n_ast, ax, ay, az, &Y);
             if (st != AG_OK) return st;
         }
 #pragma unroll
         for (int q = 0; q < AG_NPL; q++) {
             const int k = ag_planet_order(q);
             const bool on = (k == AG_SUN) ? (c.forces & AG_F_SUN) : (c.forces & AG_F_PLANETS);
-            ag_term_planet<JAC>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, J);
+            ag_term_planet<JAC>(E, on, k, dx[k], dy[k], dz[k], ri[k], ax, ay, az, &Y);
         }
+        if (JAC) ag_symjac_add(Y, J);
     }
     if (c.geocentric == 1) { ax -= ao[0]; ay -= ao[1]; az -= ao[2]; }
     acc[0] = ax; acc[1] = ay; acc[2] = az;

@@ -108,6 +108,7 @@ struct AgCoopShared {
     double pj[NV > 0 ? 4 : 1][NV > 0 ? 18 : 1][32]; /* partial Jacobians */
     double ra[3][32], rdb[3][32];                   /* |a|, |delta b6| of x, y, z at node 7 */
     double rb6[3][32];                              /* |b6| of x, y, z after convergence */
+    double pcx[8][9], pcv[8][8];                    /* predictor coefficients of nodes 1..7 of the step */
     int fin[3][32];
     int g, stop;
     int stage_fail;                                 /* a staged record copy did not complete */
@@ -395,6 +396,19 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             if (fabs(dt) >= rem_min) { hstep = dir * rem_min; last_group = true; }
             else hstep = dt;
             const bool last = live && last_group && rem == rem_min;
+            /* the predictor's coefficients of nodes 1..7, (h_n hstep)^(k+1) over
+             * the factorial-like products of IAS15's quadrature, once per step
+             * (the group's step is the block's) rather than by every warp at
+             * every node of every iteration; read after the next barrier */
+            if (tid >= 1 && tid < 8) {
+                const double s0 = hstep * ag_ias.h[tid];
+                double x = s0 * s0 * 0.5, v = s0;
+                S.pcx[tid][0] = s0; S.pcx[tid][1] = x; S.pcv[tid][0] = v;
+#pragma unroll
+                for (int k = 2; k < 9; k++) { x = x * ag_ias.fx[tid][k]; S.pcx[tid][k] = x; }
+#pragma unroll
+                for (int k = 1; k < 8; k++) { v = v * ag_ias.fv[tid][k]; S.pcv[tid][k] = v; }
+            }
 
             /* ---- node 0: accelerations at the step start, g from the predicted b */
             if (WARM && tid == 0) clk_step = clock64();
@@ -487,20 +501,15 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             while (true) {
                 for (int n = 1; n < 8; n++) {
                     const double hn = ag_ias.h[n];
-                    const double tn = t + (tc + hstep * hn);
+                    /* the product rounded on its own, as the oracle forms a node time */
+                    const double tn = t + (tc + __dmul_rn(hstep, hn));
                     AgCoopTab& TabN = S.tab[NV == 0 ? n : 0];
                     const bool build = NV != 0 || iters == 1;     /* block-uniform */
                     bad = build ? ag_coop_table_pass1<STAGE>(E, cf, tn, S.scr, TabN, tid, R, cur, &S.stage_fail) : 0;
                     n_tab += build ? 1 : 0;
                     if (!conv) {
-                        double sx[9], sv[8];
-                        sx[0] = hstep * hn;
-                        sx[1] = sx[0] * sx[0] * 0.5;
-#pragma unroll
-                        for (int k = 2; k < 9; k++) sx[k] = sx[k - 1] * ag_ias.fx[n][k];
-                        sv[0] = hstep * hn;
-#pragma unroll
-                        for (int k = 1; k < 8; k++) sv[k] = sv[k - 1] * ag_ias.fv[n][k];
+                        const double* sx = S.pcx[n];
+                        const double* sv = S.pcv[n];
                         for (int comp = 0; comp < C; comp++) {
                     if (ag_coop_owner<NV>(comp) != wid) continue;
                             double px = sx[8] * W(W_B + 6, comp);

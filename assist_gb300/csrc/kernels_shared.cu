@@ -77,16 +77,10 @@ struct ShView {
     __device__ __forceinline__ double& operator()(int f, int k, int i) const { return w[((size_t)f * 3 + k) * stride + i]; }
 };
 
-/* Predictor of component k of particle i at node `node` of a step of size
- * hstep (node 0: the start state). */
-__device__ __forceinline__ void sh_predict(const ShView& W, int i, int k, int node, double hstep) {
-    if (node == 0) {
-        W(S_XP, k, i) = W(S_X0, k, i);
-        W(S_VP, k, i) = W(S_V0, k, i);
-        return;
-    }
+/* The predictor's coefficients of node `node` (1..7) of a step of size
+ * hstep: sx[q] for x, sv[q] for v. */
+__device__ __forceinline__ void sh_predict_coeffs(int node, double hstep, double* sx, double* sv) {
     const double hn = sh_h[node];
-    double sx[9], sv[8];
     sx[0] = hstep * hn;
     sx[1] = sx[0] * sx[0] * 0.5;
 #pragma unroll
@@ -94,6 +88,16 @@ __device__ __forceinline__ void sh_predict(const ShView& W, int i, int k, int no
     sv[0] = hstep * hn;
 #pragma unroll
     for (int q = 1; q < 8; q++) sv[q] = sv[q - 1] * sh_fv[node][q];
+}
+
+/* Predictor of component k of particle i at node `node` with that node's
+ * coefficients sx, sv (node 0: the start state). */
+__device__ __forceinline__ void sh_predict(const ShView& W, int i, int k, int node, const double* sx, const double* sv) {
+    if (node == 0) {
+        W(S_XP, k, i) = W(S_X0, k, i);
+        W(S_VP, k, i) = W(S_V0, k, i);
+        return;
+    }
     double px = sx[8] * W(S_B + 6, k, i);
 #pragma unroll
     for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(S_B + j, k, i), px);
@@ -190,6 +194,7 @@ struct ShStepSmem {
     double pa[4][3][32];     /* partial accelerations of the four warps */
     double pj[4][18][32];    /* partial Jacobians; pj[0] holds their sum */
     double pja[9][32];       /* d acc / dA of the non-gravitational term (warp 0) */
+    double pcx[8][9], pcv[8][8];   /* predictor coefficients of nodes 1..7 */
     int png[32];
     unsigned long long red[3];
     int more;
@@ -278,6 +283,9 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
     const int v1 = (io.var_start && r0 < r1) ? io.var_start[r1] : 0;
     const bool jac = v1 > v0;                    /* block-uniform */
     const bool single = gridDim.x == 1;
+    /* the predictor's coefficients of the step's nodes, once per launch */
+    if (tid >= 1 && tid < 8) sh_predict_coeffs(tid, A.hstep, S.pcx[tid], S.pcv[tid]);
+    __syncthreads();
     if (A.first) {
         /* the step's eight node tables */
         int bad = 0;
@@ -306,7 +314,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
             for (int q = tid; q < (int)(sizeof(S.tab) / sizeof(double)); q += nt) dst[q] = src[q];
         }
         /* node 0: the start of the step */
-        for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, 0, A.hstep);
+        for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, 0, nullptr, nullptr);
         __syncthreads();
         sh_step_forces(S, io, A.vowner, E, c, 0, jac, v0, v1);
         for (int q = q0 + tid; q < q1; q += nt) sh_start(W, A.plist[q / 3], q % 3);
@@ -321,7 +329,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
         if (tid < 3) S.red[tid] = 0ull;
         double mdb = 0.0, ma = 0.0, mb = 0.0;
         for (int node = 1; node < 8; node++) {
-            for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, node, A.hstep);
+            for (int q = q0 + tid; q < q1; q += nt) sh_predict(W, A.plist[q / 3], q % 3, node, S.pcx[node], S.pcv[node]);
             __syncthreads();
             sh_step_forces(S, io, A.vowner, E, c, node, jac, v0, v1);
             for (int q = q0 + tid; q < q1; q += nt) sh_update(W, A.plist[q / 3], q % 3, n_real, node, mdb, ma, mb);

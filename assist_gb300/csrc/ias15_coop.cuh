@@ -109,6 +109,8 @@ struct AgCoopShared {
     double ra[3][32], rdb[3][32];                   /* |a|, |delta b6| of x, y, z at node 7 */
     double rb6[3][32];                              /* |b6| of x, y, z after convergence */
     double pcx[8][9], pcv[8][8];                    /* predictor coefficients of nodes 1..7 of the step */
+    double sdn[32], sdc[32];                        /* each lane's next-step proposal, capped and uncapped */
+    int srej[32];                                   /* and whether it rejects the step */
     int fin[3][32];
     int g, stop;
     int stage_fail;                                 /* a staged record copy did not complete */
@@ -639,22 +641,29 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             __syncthreads();
             double dt_new_l = 1e300, dt_nocap_l = 1e300;
             bool rej_l = false;
-            if (A.epsilon > 0.0 && live) {
-                double mb = 0.0;
-                for (int k = 0; k < 3; k++)
-                    if (S.rb6[k][lane] > mb) mb = S.rb6[k][lane];
-                const double err = mb / ma7;
-                const double safety = 0.25;
-                double dn;
-                if (ag_isnormal_pos(err)) dn = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
-                else dn = hstep / safety;
-                if (fabs(dn) < A.min_dt) dn = copysign(A.min_dt, dn);
-                dt_nocap_l = fabs(dn);
-                const double ratio = dn / hstep;
-                if (fabs(ratio) < safety) rej_l = true;
-                else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
-                dt_new_l = fabs(dn);
+            /* warp 0 forms each lane's proposal (the power and the divisions
+             * are FP64 work that every warp would repeat); the others read it */
+            if (wid == 0) {
+                if (A.epsilon > 0.0 && live) {
+                    double mb = 0.0;
+                    for (int k = 0; k < 3; k++)
+                        if (S.rb6[k][lane] > mb) mb = S.rb6[k][lane];
+                    const double err = mb / ma7;
+                    const double safety = 0.25;
+                    double dn;
+                    if (ag_isnormal_pos(err)) dn = pow(A.epsilon / err, 1.0 / 7.0) * hstep;
+                    else dn = hstep / safety;
+                    if (fabs(dn) < A.min_dt) dn = copysign(A.min_dt, dn);
+                    dt_nocap_l = fabs(dn);
+                    const double ratio = dn / hstep;
+                    if (fabs(ratio) < safety) rej_l = true;
+                    else if (fabs(ratio) > 1.0 / safety) dn = hstep / safety;
+                    dt_new_l = fabs(dn);
+                }
+                S.sdn[lane] = dt_new_l; S.sdc[lane] = dt_nocap_l; S.srej[lane] = rej_l ? 1 : 0;
             }
+            __syncthreads();
+            if (wid != 0) { dt_new_l = S.sdn[lane]; dt_nocap_l = S.sdc[lane]; rej_l = S.srej[lane] != 0; }
             if (live && !last_group && A.epsilon > 0.0 && A.dt_floor > 0.0 && dt_nocap_l < A.dt_floor) {
                 /* step underflow: this lane's particle is hitting a body; it stops
                  * (state of the step start) and the group goes on without it.  Not

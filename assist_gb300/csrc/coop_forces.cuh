@@ -395,7 +395,7 @@ __device__ __forceinline__ void ag_coop_ast_rel(const AgCoopTab& CT, bool geo, i
 template <bool JAC, bool F2 = true>
 __device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoopTab& CT, bool geo, bool on_ast,
                                                   const double* x, int m0, int m1, double& ax, double& ay, double& az,
-                                                  double (*J)[6]) {
+                                                  double (*J)[6], const AgF2* xf_in = nullptr) {
     if (JAC || !F2) {
         AgSymJac Y = {{0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, 0.0};
 #pragma unroll 1
@@ -412,7 +412,10 @@ __device__ __forceinline__ void ag_coop_asteroids(const DevEphem& E, const AgCoo
         return;
     }
     if (!on_ast) return;
-    const AgF2 xf[3] = {ag_f2_of(x[0]), ag_f2_of(x[1]), ag_f2_of(x[2])};
+    /* the position as float pairs: from the caller (split once by the
+     * warp that predicted it) or here */
+    const AgF2 xf[3] = {xf_in ? xf_in[0] : ag_f2_of(x[0]), xf_in ? xf_in[1] : ag_f2_of(x[1]),
+                        xf_in ? xf_in[2] : ag_f2_of(x[2])};
     AgF2 sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f}, sz = {0.0f, 0.0f};
 #pragma unroll 1
     for (int m = m0; m < m1; m++) {
@@ -481,7 +484,7 @@ template <bool JAC, bool F2 = true>
 __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, const DevEphem& E, const ForceCfg& c,
                                                   const double* x, const double* v, const double* A, double* acc,
                                                   double (*J)[6], double (*JA_out)[3] = nullptr,
-                                                  bool* ng_out = nullptr) {
+                                                  bool* ng_out = nullptr, const AgF2* xf = nullptr) {
     const AgTable& T = CT.T;
     const TableBodies B(T);
     const PlanetState& P = T.P;
@@ -542,7 +545,7 @@ __device__ __forceinline__ int ag_coop_force_part(int w, const AgCoopTab& CT, co
         const int h = (E.n_ast + 1) / 2;
         if (direct && (on_ast || JAC))
             ag_coop_asteroids<JAC, F2>(E, CT, c.geocentric == 1, on_ast, x, w == 2 ? 0 : h, w == 2 ? h : E.n_ast, ax,
-                                       ay, az, J);
+                                       ay, az, J, xf);
         if (w == 2 && (c.forces & AG_F_EARTH_H)) {
             double dx, dy, dz, ri;
             ag_coop_sep(CT, x, AG_EAR, dx, dy, dz, ri);

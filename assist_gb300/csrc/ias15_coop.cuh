@@ -109,6 +109,8 @@ struct AgCoopShared {
     double ra[3][32], rdb[3][32];                   /* |a|, |delta b6| of x, y, z at node 7 */
     double rb6[3][32];                              /* |b6| of x, y, z after convergence */
     double pcx[8][9], pcv[8][8];                    /* predictor coefficients of nodes 1..7 of the step */
+    double ptn[8];                                  /* and the node times */
+    AgF2 xsf[NV == 0 ? 3 : 1][32];                  /* the state's position as float pairs (asteroid terms) */
     double sdn[32], sdc[32];                        /* each lane's next-step proposal, capped and uncapped */
     int srej[32];                                   /* and whether it rejects the step */
     int fin[3][32];
@@ -403,6 +405,8 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
              * (the group's step is the block's) rather than by every warp at
              * every node of every iteration; read after the next barrier */
             if (tid >= 1 && tid < 8) {
+                /* the product rounded on its own, as the oracle forms a node time */
+                S.ptn[tid] = t + (tc + __dmul_rn(hstep, ag_ias.h[tid]));
                 const double s0 = hstep * ag_ias.h[tid];
                 double x = s0 * s0 * 0.5, v = s0;
                 S.pcx[tid][0] = s0; S.pcx[tid][1] = x; S.pcv[tid][0] = v;
@@ -418,7 +422,10 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             n_tab++;
             if (live)
                 for (int comp = 0; comp < C; comp++)
-                    if (ag_coop_owner<NV>(comp) == wid) { S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp); }
+                    if (ag_coop_owner<NV>(comp) == wid) {
+                        S.xs[comp][lane] = W(W_X0, comp); S.vs[comp][lane] = W(W_V0, comp);
+                        if constexpr (NV == 0 && !WARM) S.xsf[comp][lane] = ag_f2_of(W(W_X0, comp));
+                    }
             bad = __syncthreads_or(bad);
             if (bad) { pstat = S.stage_fail ? AG_ST_TIMEOUT : AG_ST_COVERAGE; finish_now = live; continue; }
             ag_coop_table_pass2(E, cf, t, Tab, S.scr, tid);
@@ -441,7 +448,9 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                     if constexpr (NV == 0)
                         ag_coop_force_split01(wid, live, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                 } else if (live) {
-                    fst = ag_coop_force_part<false, !WARM>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                    const AgF2 xf3[3] = {S.xsf[0][lane], S.xsf[NV == 0 ? 1 : 0][lane], S.xsf[NV == 0 ? 2 : 0][lane]};
+                    fst = ag_coop_force_part<false, !WARM>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr,
+                                                           nullptr, nullptr, (NV == 0 && !WARM) ? xf3 : nullptr);
                 }
                 if (live) {
                     S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
@@ -502,9 +511,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             bool cov = false;
             while (true) {
                 for (int n = 1; n < 8; n++) {
-                    const double hn = ag_ias.h[n];
-                    /* the product rounded on its own, as the oracle forms a node time */
-                    const double tn = t + (tc + __dmul_rn(hstep, hn));
+                    const double tn = S.ptn[n];
                     AgCoopTab& TabN = S.tab[NV == 0 ? n : 0];
                     const bool build = NV != 0 || iters == 1;     /* block-uniform */
                     bad = build ? ag_coop_table_pass1<STAGE>(E, cf, tn, S.scr, TabN, tid, R, cur, &S.stage_fail) : 0;
@@ -519,7 +526,9 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                             for (int j = 5; j >= 0; j--) px = fma(sx[j + 2], W(W_B + j, comp), px);
                             px = fma(sx[1], W(W_A0, comp), px);
                             px = fma(sx[0], W(W_V0, comp), px);
-                            S.xs[comp][lane] = W(W_X0, comp) + (px + W(W_XC, comp));
+                            const double xn = W(W_X0, comp) + (px + W(W_XC, comp));
+                            S.xs[comp][lane] = xn;
+                            if constexpr (NV == 0 && !WARM) S.xsf[comp][lane] = ag_f2_of(xn);
                             double pv = sv[7] * W(W_B + 6, comp);
 #pragma unroll
                             for (int j = 5; j >= 0; j--) pv = fma(sv[j + 1], W(W_B + j, comp), pv);
@@ -550,7 +559,9 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                             if constexpr (NV == 0)
                                 ag_coop_force_split01(wid, !conv, S.seps, lane, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                         } else if (!conv) {
-                            ag_coop_force_part<false, !WARM>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr);
+                            const AgF2 xf3[3] = {S.xsf[0][lane], S.xsf[NV == 0 ? 1 : 0][lane], S.xsf[NV == 0 ? 2 : 0][lane]};
+                            ag_coop_force_part<false, !WARM>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr,
+                                                             nullptr, nullptr, (NV == 0 && !WARM) ? xf3 : nullptr);
                         }
                         if (!conv) {
                             S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];

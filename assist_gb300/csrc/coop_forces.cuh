@@ -14,6 +14,7 @@
 #define ASSIST_GB300_COOP_FORCES_CUH
 
 #include "device_forces.cuh"
+#include "ieee_convert.cuh"
 #include "warp_table.cuh"
 
 #ifndef AG_FULL
@@ -135,11 +136,13 @@ __device__ __forceinline__ AgF2 ag_f2_mul(AgF2 a, AgF2 b) {
     return ag_f2_fast(p, e);
 }
 __device__ __forceinline__ AgF2 ag_f2_neg(AgF2 a) { return {-a.h, -a.l}; }
+/* The split of a double and the sum back, their conversions on the integer
+ * pipes (bit for bit the hardware's, which would occupy the FP64 pipe). */
 __device__ __forceinline__ AgF2 ag_f2_of(double x) {
-    const float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};
+    const float h = ag_d2f_int(x);
+    return {h, ag_d2f_int(x - ag_f2d_int(h))};
 }
-__device__ __forceinline__ double ag_f2_to(AgF2 a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ double ag_f2_to(AgF2 a) { return ag_f2d_int(a.h) + ag_f2d_int(a.l); }
 /* 1/sqrt(x): the FP32 estimate y0, then one Newton step in double-float,
  * y = y0 + y0 (1 - x y0^2) / 2 (relative error about 1.5 e0^2, a few 1e-14). */
 __device__ __forceinline__ AgF2 ag_f2_rsqrt(AgF2 x) {

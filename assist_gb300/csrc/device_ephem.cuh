@@ -95,7 +95,15 @@ struct DevEphem {
  * maxima of |a| and |b|): at least the smallest normal double and finite;
  * false for 0, subnormals, Inf and NaN. */
 __device__ __forceinline__ bool ag_isnormal_pos(double a) {
-    return a >= 2.2250738585072014e-308 && a <= 1.7976931348623157e308;
+    /* a >= DBL_MIN && a <= DBL_MAX, on the high word (an integer compare
+     * rather than two FP64 ones): sign clear and exponent field 1..2046 */
+    return (unsigned)__double2hiint(a) - 0x00100000u <= 0x7FEFFFFFu - 0x00100000u;
+}
+/* The larger of two non-negative doubles (or zero and a normal value): their
+ * bit patterns order as integers do, compared on the integer pipes. */
+__device__ __forceinline__ double ag_max_nonneg(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    return __longlong_as_double(ia > ib ? ia : ib);
 }
 
 /* Sub-interval b of tt = record fraction x niv and the integer part fl with

@@ -607,8 +607,8 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                 if (!conv) {
                     double maxa = 0.0, maxdb = 0.0;
                     for (int k = 0; k < 3; k++) {
-                        if (S.ra[k][lane] > maxa) maxa = S.ra[k][lane];
-                        if (S.rdb[k][lane] > maxdb) maxdb = S.rdb[k][lane];
+                        maxa = ag_max_nonneg(maxa, S.ra[k][lane]);
+                        maxdb = ag_max_nonneg(maxdb, S.rdb[k][lane]);
                     }
                     ma7 = maxa;
                     const double pc_err = maxdb / maxa;
@@ -657,8 +657,7 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
             if (wid == 0) {
                 if (A.epsilon > 0.0 && live) {
                     double mb = 0.0;
-                    for (int k = 0; k < 3; k++)
-                        if (S.rb6[k][lane] > mb) mb = S.rb6[k][lane];
+                    for (int k = 0; k < 3; k++) mb = ag_max_nonneg(mb, S.rb6[k][lane]);
                     const double err = mb / ma7;
                     const double safety = 0.25;
                     double dn;

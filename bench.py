@@ -79,10 +79,10 @@ IAS_PER_STEP = 3 * (2 * 9 + 2 * 8 + 8 + 7 * 8)
 
 # From one ncu capture of the block-cooperative kernel (three-blocks-per-SM
 # build) on the 32,768-particle case of this workload
-# (profiles/ag_k_coop_32768_mixture_1yr.md: 4.62 MB read + written for 11.97M
+# (profiles/ag_k_coop_32768_mixture_1yr.md: 4.64 MB read + written for 11.97M
 # particle-days): DRAM bytes per particle-day of a launch, scaled to a full
 # launch by its particle-days.
-DRAM_BYTES_PER_PARTICLE_DAY = 0.386
+DRAM_BYTES_PER_PARTICLE_DAY = 0.388
 
 
 def _synth():

@@ -10,15 +10,18 @@
  * kernel (sh_k_step) whose 128-thread blocks each own 32 real particles and
  * their variational particles and build the step's eight body tables once.
  * The update of node 7 also reduces max|delta b6|, max|a| and max|b6| over
- * the real particles (the global error measures of adaptive_mode = 1).  With
- * several blocks a launch is one iteration and the host reads the three
- * maxima back to decide convergence; with one block (up to 32 real
- * particles) a launch is the whole predictor-corrector loop of the step.  The
- * host then decides acceptance and the next step size, with the same rules as
- * the batched kernel (kernels_ias15.cu).
+ * the real particles (the global error measures of adaptive_mode = 1).  A
+ * launch is the whole predictor-corrector loop of the step when the
+ * simulation has one block (up to 32 real particles) or when all its blocks
+ * fit on the device at once (a cooperative launch whose blocks meet at a
+ * bounded grid barrier after each iteration); otherwise a launch is one
+ * iteration and the host reads the three maxima back to decide convergence.
+ * The host then decides acceptance and the next step size, with the same
+ * rules as the batched kernel (kernels_ias15.cu).
  */
 #include <cuda_runtime.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -166,9 +169,13 @@ __device__ __forceinline__ void sh_update(const ShView& W, int i, int k, int n_r
  * (max|delta b6|, max|a|, max|b6|; bit patterns of non-negative doubles
  * order like unsigned integers) go to red[0..2].
  *
- * Several blocks: one iteration per launch and the host decides convergence;
- * the first launch of a step (`first`: node 0 and the tables) leaves the
- * tables in gtab for the launches after it.  One block (up to 32 real
+ * Several blocks: in one cooperative launch when every block fits on the
+ * device at once (each block builds the tables; after each iteration the
+ * blocks' maxima meet in global memory across a bounded grid barrier and
+ * every block takes the same convergence decision), else one iteration per
+ * launch with the host deciding convergence, the first launch of a step
+ * (`first`: node 0 and the tables) leaving the tables in gtab for the
+ * launches after it.  One block (up to 32 real
  * particles): every iteration of the step in one launch, with the host's
  * convergence rule (relative corrector change below 1e-16, no longer
  * decreasing after two iterations, or 12 iterations) and the iteration count
@@ -180,8 +187,11 @@ struct ShStepArgs {
     const int* vowner;       /* real particle of each variational entry of io */
     const int* plist;
     const int* pstart;
-    unsigned long long* red;
-    AgCoopTab* gtab;         /* the step's eight node tables (several blocks) */
+    unsigned long long* red; /* [0..3] the step's maxima and iterations; [4..12] three rotating
+                                reduction buffers of a cooperative launch */
+    AgCoopTab* gtab;         /* the step's eight node tables (several blocks, one launch per iteration) */
+    unsigned* bar;           /* grid barrier of a cooperative launch: arrivals, generation, gave up */
+    int coop;                /* several blocks in one cooperative launch run the whole step */
     double tn[8];            /* node times: t + (tc + hstep h_n), from the host */
     double hstep;
     int first;
@@ -198,7 +208,41 @@ struct ShStepSmem {
     int png[32];
     unsigned long long red[3];
     int more;
+    int bar_ok;
 };
+
+/* Barrier of all blocks of a cooperative launch (the runtime makes every
+ * block resident or refuses the launch).  Thread 0 of each block reads the
+ * generation, then counts its arrival; the last arrival resets the count and
+ * advances the generation, the others poll it.  A block that has polled
+ * SH_BAR_POLLS times stops waiting, records that in bar[2] and returns
+ * false; its block then leaves the kernel, and the other blocks stop at
+ * their own limits, so the launch always ends. */
+#define SH_BAR_POLLS (1 << 21)
+__device__ __forceinline__ bool sh_grid_sync(unsigned* bar, int* ok_smem) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            int polls = 0;
+            while (*vgen == gen) {
+                if (++polls > SH_BAR_POLLS) { ok = 0; atomicExch(&bar[2], 1u); break; }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        *ok_smem = ok;
+    }
+    __syncthreads();
+    return *ok_smem != 0;
+}
 
 /* Accelerations of the block's particles at node n (table S.tab[n]) into
  * io.a; ends with a block barrier. */
@@ -283,6 +327,7 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
     const int v1 = (io.var_start && r0 < r1) ? io.var_start[r1] : 0;
     const bool jac = v1 > v0;                    /* block-uniform */
     const bool single = gridDim.x == 1;
+    const bool whole = single || A.coop;         /* the launch runs the step's whole corrector loop */
     /* the predictor's coefficients of the step's nodes, once per launch */
     if (tid >= 1 && tid < 8) sh_predict_coeffs(tid, A.hstep, S.pcx[tid], S.pcv[tid]);
     __syncthreads();
@@ -302,13 +347,14 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
             for (int n = wid; n < 8; n += 4) ag_coop_eih_sources(E, c, S.tab[n].T, lane);
         bad = __syncthreads_or(bad);
         if (bad) {
+            /* every block builds the same tables: all of them leave here */
             if (tid == 0) {
                 if (n_real > 0) atomicMax(io.status, (int)AG_ERR_COVERAGE);
-                if (single) { A.red[0] = A.red[1] = A.red[2] = 0ull; A.red[3] = 1ull; }
+                if (whole && blockIdx.x == 0) { A.red[0] = A.red[1] = A.red[2] = 0ull; A.red[3] = 1ull; }
             }
             return;
         }
-        if (!single && blockIdx.x == 0) {
+        if (!whole && blockIdx.x == 0) {
             const double* src = reinterpret_cast<const double*>(S.tab);
             double* dst = reinterpret_cast<double*>(A.gtab);
             for (int q = tid; q < (int)(sizeof(S.tab) / sizeof(double)); q += nt) dst[q] = src[q];
@@ -345,16 +391,27 @@ __global__ void __launch_bounds__(128) sh_k_step(const DevEphem* __restrict__ Ep
             atomicMax(&S.red[2], (unsigned long long)__double_as_longlong(mb));
         }
         __syncthreads();
-        if (!single) {
+        if (!whole) {
             if (tid < 3) atomicMax(&A.red[tid], S.red[tid]);
             return;
+        }
+        if (A.coop) {
+            /* the maxima over all blocks: buffer iters % 3 collects this
+             * iteration's, block 0 clears the next one (last read two
+             * barriers ago), every block reads the result after the barrier */
+            unsigned long long* rb = A.red + 4 + 3 * (iters % 3);
+            if (tid < 3) atomicMax(&rb[tid], S.red[tid]);
+            if (blockIdx.x == 0 && tid < 3) A.red[4 + 3 * ((iters + 1) % 3) + tid] = 0ull;
+            if (!sh_grid_sync(A.bar, &S.bar_ok)) return;
+            if (tid < 3) S.red[tid] = atomicOr(&rb[tid], 0ull);
+            __syncthreads();
         }
         if (tid == 0) {
             const double pc_err = __longlong_as_double((long long)S.red[0]) / __longlong_as_double((long long)S.red[1]);
             const bool conv = (pc_err < 1e-16) || (iters > 2 && pc_last <= pc_err) || (iters >= 12);
             S.more = !conv;
             pc_last = pc_err;
-            if (conv) {
+            if (conv && blockIdx.x == 0) {
                 A.red[0] = S.red[0]; A.red[1] = S.red[1]; A.red[2] = S.red[2];
                 A.red[3] = (unsigned long long)iters;
             }
@@ -527,7 +584,9 @@ struct AgSharedSim {
     size_t pcap = 0;
     int nblocks = 1;
     AgCoopTab* d_tab = nullptr;   /* the step's node tables (several blocks) */
-    unsigned long long* d_red = nullptr;
+    unsigned long long* d_red = nullptr;  /* 16 words: maxima, iterations, rotating buffers */
+    unsigned* d_bar = nullptr;    /* grid barrier of the cooperative step launch */
+    int coop_blocks = -1;         /* blocks a cooperative step launch can hold (-1: not yet asked) */
     int* d_status = nullptr;
     cudaStream_t stream = nullptr;
     double* h_pin = nullptr;      /* pinned staging, 6*cap doubles */
@@ -549,6 +608,7 @@ void ag_shared_free(AgSharedSim* s) {
     if (s->d_vowner) cudaFree(s->d_vowner);
     if (s->d_tab) cudaFree(s->d_tab);
     if (s->d_red) cudaFree(s->d_red);
+    if (s->d_bar) cudaFree(s->d_bar);
     if (s->d_status) cudaFree(s->d_status);
     if (s->h_pin) cudaFreeHost(s->h_pin);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -558,7 +618,8 @@ void ag_shared_free(AgSharedSim* s) {
 static int sh_reserve(AgSharedSim* s, int n) {
     if (!s->stream && ag_cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream")) return 1;
     if (!s->d_red) {
-        if (ag_cuda_check(cudaMalloc(&s->d_red, 4 * sizeof(unsigned long long)), "cudaMalloc(red)")) return 1;
+        if (ag_cuda_check(cudaMalloc(&s->d_red, 16 * sizeof(unsigned long long)), "cudaMalloc(red)")) return 1;
+        if (ag_cuda_check(cudaMalloc(&s->d_bar, 4 * sizeof(unsigned)), "cudaMalloc(barrier)")) return 1;
         if (ag_cuda_check(cudaMalloc(&s->d_status, sizeof(int)), "cudaMalloc(status)")) return 1;
         if (ag_cuda_check(cudaMalloc(&s->d_tab, 8 * sizeof(AgCoopTab)), "cudaMalloc(node tables)")) return 1;
     }
@@ -756,6 +817,21 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
     const double eps = r->ri_ias15.epsilon, min_dt = r->ri_ias15.min_dt;
     unsigned long long red[4];
     int hstat = 0;
+    unsigned bar_gave_up = 0;
+    /* several blocks run a step in one cooperative launch when all of them
+     * fit on the device at once; otherwise one launch per iteration
+     * (ASSIST_GB300_SHARED_COOP=0 forces that path) */
+    if (s->coop_blocks < 0) {
+        int dev = 0, sms = 0, bps = 0, can = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&can, cudaDevAttrCooperativeLaunch, dev);
+        if (const char* ev = getenv("ASSIST_GB300_SHARED_COOP"))
+            if (atoi(ev) == 0) can = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sh_k_step, tpb, sizeof(ShStepSmem)) != cudaSuccess) bps = 0;
+        s->coop_blocks = can ? bps * sms : 0;
+    }
+    const bool use_coop = nb > 1 && nb <= s->coop_blocks;
     long long steps = 0;
     while (s->t != tmax) {
         const double rem = (tmax - s->t) - s->tc;
@@ -765,19 +841,39 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
         ShStepArgs A;
         A.W = W; A.io = io; A.vowner = s->d_vowner; A.plist = s->d_plist; A.pstart = s->d_pstart; A.red = s->d_red;
         A.gtab = s->d_tab;
+        A.bar = s->d_bar;
+        A.coop = 0;
         A.hstep = hstep;
         A.tn[0] = s->t;
         for (int node = 1; node < 8; node++) A.tn[node] = s->t + (s->tc + hstep * h_nodes[node]);
         A.first = 1;
         cudaMemsetAsync(s->d_status, 0, sizeof(int), st);
         int iters = 1;
-        if (nb == 1) {
-            /* one block: the whole predictor-corrector loop in one launch */
-            sh_k_step<<<1, tpb, sizeof(ShStepSmem), st>>>(E.self_dev, c, A);
-            if (ag_cuda_check(cudaGetLastError(), "IAS15 step kernel")) return 1;
+        if (nb == 1 || use_coop) {
+            /* one block, or every block resident in a cooperative launch: the
+             * whole predictor-corrector loop in one launch */
+            if (nb == 1) {
+                sh_k_step<<<1, tpb, sizeof(ShStepSmem), st>>>(E.self_dev, c, A);
+                if (ag_cuda_check(cudaGetLastError(), "IAS15 step kernel")) return 1;
+            } else {
+                A.coop = 1;
+                cudaMemsetAsync(s->d_red, 0, 16 * sizeof(unsigned long long), st);
+                cudaMemsetAsync(s->d_bar, 0, 4 * sizeof(unsigned), st);
+                const DevEphem* ep = E.self_dev;
+                ForceCfg cc = c;
+                void* args[] = {(void*)&ep, (void*)&cc, (void*)&A};
+                if (ag_cuda_check(cudaLaunchCooperativeKernel((const void*)sh_k_step, nb, tpb, args, sizeof(ShStepSmem), st),
+                                  "IAS15 step kernel (cooperative)"))
+                    return 1;
+                cudaMemcpyAsync(&bar_gave_up, s->d_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+            }
             cudaMemcpyAsync(red, s->d_red, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
             cudaMemcpyAsync(&hstat, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
             if (ag_cuda_check(cudaStreamSynchronize(st), "IAS15 step")) return 1;
+            if (bar_gave_up) {
+                ag_set_error("IAS15 step kernel: a block stopped waiting at the grid barrier");
+                return 1;
+            }
             iters = (int)red[3];
             out->evals += 1 + 7 * (long long)iters;
             if (hstat != 0) out->status = hstat;

@@ -162,6 +162,38 @@ def test_shared_step_drop_in_vs_oracle(synth_files):
     ex.detach(sim); sim.free()
 
 
+def test_shared_step_cooperative_launch_equals_per_iteration(synth_files, monkeypatch):
+    """Several blocks run a step in one cooperative launch (their maxima meet
+    across a grid barrier and every block takes the convergence decision) or
+    one launch per iteration (the host decides): the same arithmetic and the
+    same decisions, so the same end states bit for bit, real and variational
+    particles (5 blocks, some with variational particles)."""
+    from assist_gb300 import Extras, Simulation, synth
+    pl, ast, system = synth_files
+    eph = _eph((pl, ast))
+    pop = synth.population(system, "neo", 150, seed=12, t0=8000.0)
+
+    def run():
+        sim = Simulation.create(); ex = Extras(sim, eph)
+        for s in pop.state:
+            sim.add(*s)
+        for i in range(0, 150, 25):
+            for k in range(6):
+                setattr(sim.particle(sim.add_variation(i)), ["x", "y", "z", "vx", "vy", "vz"][k], 1.0)
+        sim.t = 8000.0
+        sim.integrate(8150.0)
+        g = np.array([[p.x, p.y, p.z, p.vx, p.vy, p.vz] for p in sim.particles])
+        out = (sim.status, sim.steps_done, g)
+        ex.detach(sim); sim.free()
+        return out
+
+    st_c, n_c, g_c = run()
+    monkeypatch.setenv("ASSIST_GB300_SHARED_COOP", "0")
+    st_i, n_i, g_i = run()
+    assert st_c == 0 and st_i == 0 and n_c == n_i
+    assert np.array_equal(g_c, g_i)
+
+
 @pytest.mark.parametrize("n", [8, 40])
 def test_shared_step_nongrav_variational_vs_oracle(synth_files, n):
     """Shared-step drop-in with Marsden parameters on every real particle and

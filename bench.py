@@ -414,7 +414,8 @@ def shared_configs(eph, system, o_cpu, runs):
                 "description": "one REBOUND simulation of 1,024 main-belt particles sharing the IAS15 step "
                                "(epsilon 1e-9), 365.25 days, through sim.integrate with ASSIST attached",
                 "n_particles": 1024, "value": pdays / np.mean(walls) if walls else None, "unit": UNIT,
-                "wall_s": float(np.mean(walls)) if walls else None, "runs": len(walls), "steps": int(steps),
+                "wall_s": float(np.mean(walls)) if walls else None, "runs": len(walls),
+                "wall_s_runs": [float(w) for w in walls], "steps": int(steps),
                 "us_per_step": 1e6 * float(np.mean(walls)) / max(steps, 1) if walls else None,
                 "parity": {"max_au": float(dx.max()), "median_au": float(np.median(dx)),
                            "oracle_steps": info["accepted"]},

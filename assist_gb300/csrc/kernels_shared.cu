@@ -831,7 +831,7 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, sh_k_step, tpb, sizeof(ShStepSmem)) != cudaSuccess) bps = 0;
         s->coop_blocks = can ? bps * sms : 0;
     }
-    const bool use_coop = nb > 1 && nb <= s->coop_blocks;
+    bool use_coop = nb > 1 && nb <= s->coop_blocks;
     long long steps = 0;
     while (s->t != tmax) {
         const double rem = (tmax - s->t) - s->tc;
@@ -862,9 +862,17 @@ int ag_shared_integrate(AgSharedSim* s, const DevEphem& E, const ForceCfg& c, st
                 const DevEphem* ep = E.self_dev;
                 ForceCfg cc = c;
                 void* args[] = {(void*)&ep, (void*)&cc, (void*)&A};
-                if (ag_cuda_check(cudaLaunchCooperativeKernel((const void*)sh_k_step, nb, tpb, args, sizeof(ShStepSmem), st),
-                                  "IAS15 step kernel (cooperative)"))
-                    return 1;
+                const cudaError_t le =
+                    cudaLaunchCooperativeKernel((const void*)sh_k_step, nb, tpb, args, sizeof(ShStepSmem), st);
+                if (le == cudaErrorCooperativeLaunchTooLarge) {
+                    /* the blocks no longer fit at once: this step and the
+                     * rest in one launch per iteration */
+                    cudaGetLastError();
+                    s->coop_blocks = 0;
+                    use_coop = false;
+                    continue;
+                }
+                if (ag_cuda_check(le, "IAS15 step kernel (cooperative)")) return 1;
                 cudaMemcpyAsync(&bar_gave_up, s->d_bar + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
             }
             cudaMemcpyAsync(red, s->d_red, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);

@@ -448,9 +448,14 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                     if constexpr (NV == 0)
                         ag_coop_force_split01(wid, live, S.seps, lane, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                 } else if (live) {
-                    const AgF2 xf3[3] = {S.xsf[0][lane], S.xsf[NV == 0 ? 1 : 0][lane], S.xsf[NV == 0 ? 2 : 0][lane]};
+                    AgF2 xf3[3];
+                    const AgF2* xfp = nullptr;          /* the float-pair position, where it was split */
+                    if constexpr (NV == 0 && !WARM) {
+                        xf3[0] = S.xsf[0][lane]; xf3[1] = S.xsf[1][lane]; xf3[2] = S.xsf[2][lane];
+                        xfp = xf3;
+                    }
                     fst = ag_coop_force_part<false, !WARM>(wid, Tab, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr,
-                                                           nullptr, nullptr, (NV == 0 && !WARM) ? xf3 : nullptr);
+                                                           nullptr, nullptr, xfp);
                 }
                 if (live) {
                     S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
@@ -559,9 +564,14 @@ __global__ void __launch_bounds__(128, OCC) ag_k_coop(const DevEphem* __restrict
                             if constexpr (NV == 0)
                                 ag_coop_force_split01(wid, !conv, S.seps, lane, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc);
                         } else if (!conv) {
-                            const AgF2 xf3[3] = {S.xsf[0][lane], S.xsf[NV == 0 ? 1 : 0][lane], S.xsf[NV == 0 ? 2 : 0][lane]};
+                            AgF2 xf3[3];
+                            const AgF2* xfp = nullptr;
+                            if constexpr (NV == 0 && !WARM) {
+                                xf3[0] = S.xsf[0][lane]; xf3[1] = S.xsf[1][lane]; xf3[2] = S.xsf[2][lane];
+                                xfp = xf3;
+                            }
                             ag_coop_force_part<false, !WARM>(wid, TabN, E, cf, xp, vp, has_prm ? prm : nullptr, acc, nullptr,
-                                                             nullptr, nullptr, (NV == 0 && !WARM) ? xf3 : nullptr);
+                                                             nullptr, nullptr, xfp);
                         }
                         if (!conv) {
                             S.pa[wid][0][lane] = acc[0]; S.pa[wid][1][lane] = acc[1]; S.pa[wid][2][lane] = acc[2];
